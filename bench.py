@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FWI engine: one VI iteration's misfit + gradient batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--config cfg2]
+
+A "step" is one pass of the forward/adjoint path over one batch: every
+(sample, shot) solve of the configuration (default: the batched VI
+iteration, 64 samples x 20 shots on a 200x400 grid, nt 3000), followed by the
+per-sample gradient and FP64 misfit reductions.  Inputs are seeded synthetic
+models of the configuration's shapes (no dataset is shipped).
+
+Printed as one JSON line by rank 0:
+  value   useful FD cell-updates/s (2*ns*nt*ntp per sample), device-timed,
+          inputs resident in HBM; max over ranks, summed over replicas
+  e2e     the same metric through the public Posterior.fwi call with host
+          float64 samples in and host loss/gradient out (copies timed)
+  roofline  the time-step kernel: algorithmic bytes per launch / its average
+          launch time (CUDA events around the step loops), against the
+          measured HBM copy bandwidth
+  cpu_baseline  the oracle port of the reference solver (FP32, OpenMP on all
+          host cores) on a bounded sample of the same workload
+Multi-GPU: replicas only -- each rank solves its own batch, no collective on
+the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    ap.add_argument("--cpu-shots", type=int, default=2, help="shots in the bounded CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--hbm-budget-gb", type=float, default=None)
+    return ap.parse_args()
+
+
+def workload(name: str):
+    from geopvi_gb300 import workloads
+    return {"cfg1": workloads.cfg1, "cfg2": workloads.cfg2, "cfg3": workloads.cfg3}[name]()
+
+
+WORKLOAD_NAMES = {
+    "cfg1": "plain fwi2d misfit+gradient, 120x250 grid, nt 2000, 10 shots, 250 receivers, 4 samples",
+    "cfg2": "batched VI iteration, 200x400 grid, nt 3000, 20 shots, 400 receivers, 64 samples",
+    "cfg3": "autograd batch, 300x600 grid, nt 4000, dt 0.8 ms, 32 shots, 600 receivers, 16 samples",
+}
+
+
+def cell_updates_per_sample(p) -> int:
+    return 2 * p.ns * p.nt * p.ntp
+
+
+def algorithmic_bytes_per_sample(p) -> int:
+    """16 B per propagation cell-update (read p0, p1, v*dt; write p2) plus,
+    per interior cell per stored step, 4 B written forward and 12 B in the
+    adjoint (read the stored field, read-modify-write the accumulator)."""
+    return p.ns * (2 * p.nt * 16 * p.ntp + p.nt_save * 16 * p.ncell)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port (or the compiled reference where it loads)
+# ---------------------------------------------------------------------------
+def cpu_sample(p, vel: np.ndarray, obs_shots: np.ndarray, shots: int):
+    """Time the reference arithmetic on the host for `shots` shots of one
+    sample; returns (cell-updates/s, seconds, kind, threads, description)."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    O.set_threads(threads)
+    sub = p.replace(ns=shots)
+    op = O.Params(**{k: getattr(sub, k) for k in O.INT_FIELDS + O.FLOAT_FIELDS})
+    obs = np.ascontiguousarray(obs_shots.reshape(p.ns, p.nt, p.nr)[:shots]).ravel()
+    kind = "port"
+    t0 = time.perf_counter()
+    if O.ref_available():
+        try:
+            O.ref_fwi(op, vel.astype(np.float64), obs, 1)
+            kind = "reference"
+        except OSError:
+            O.fwi_f32(op, vel, obs, 1)
+    else:
+        O.fwi_f32(op, vel, obs, 1)
+    dt = time.perf_counter() - t0
+    cu = 2 * shots * p.nt * p.ntp
+    desc = (f"1 sample x {shots} of {p.ns} shots ({p.nz}x{p.nx}, nt {p.nt}); "
+            f"{'compiled reference fdtd2D_modelling.c' if kind == 'reference' else 'FP32 C++ port of fdtd2D_modelling.c'}"
+            f", OpenMP {O.get_threads()} threads; cost is linear in shots and samples")
+    return cu / dt, dt, kind, O.get_threads(), desc
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = workload(args.config)
+    p = w.params
+    # observed data from the truth on the host, with the same port (bounded: the sampled shots only)
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    sub = p.replace(ns=args.cpu_shots)
+    op = O.Params(**{k: getattr(sub, k) for k in O.INT_FIELDS + O.FLOAT_FIELDS})
+    obs_sub = O.forward_f32(op, w.truth)
+    obs = np.zeros(p.data_len, np.float32)
+    obs[: obs_sub.size] = obs_sub
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        v, dt, kind, threads, desc = cpu_sample(p, w.samples[i % len(w.samples)], obs, args.cpu_shots)
+        if i >= args.warmup:
+            vals.append((v, dt))
+        info = (kind, threads, desc)
+    value = float(np.mean([v for v, _ in vals]))
+    ms = float(np.mean([dt for _, dt in vals]) * 1e3)
+    kind, threads, desc = info
+    out = {
+        "impl": "reference", "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": value,
+        "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD_NAMES[args.config], "sample": desc},
+        "sample_gradients_per_s": value / cell_updates_per_sample(p),
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": kind, "sample": desc},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def load_traffic(p, nres_avg: float):
+    """DRAM bytes per step launch from the committed ncu summary, scaled to
+    this workload by padded cells per launch (traffic grows in proportion)."""
+    path = os.path.join(REPO, "profiles", "k_step_traffic.json")
+    if not os.path.exists(path):
+        return None
+    try:
+        t = json.load(open(path))
+        per_cell = float(t["dram_bytes_per_launch"]) / float(t["padded_cells_per_launch"])
+        return per_cell * p.ntp * nres_avg
+    except (KeyError, ValueError, ZeroDivisionError):
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    from geopvi_gb300.engine import Fwi2dEngine
+    w = workload(args.config)
+    p = w.params
+    budget = int(args.hbm_budget_gb * 2**30) if args.hbm_budget_gb else None
+    eng = Fwi2dEngine(p, device=dev, graph=False, hbm_budget=budget)
+    vel = torch.from_numpy(w.samples).to(dev)
+    zeros = torch.zeros(p.data_len, dtype=torch.float32, device=dev)
+    obs = eng.run(torch.from_numpy(w.truth).to(dev).unsqueeze(0), zeros, forward_only=True).syn[0].clone()
+    nsamples = vel.shape[0]
+    resident = eng.resident_for(nsamples)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        eng.run(vel, obs, profile=True)
+    torch.cuda.synchronize(dev)
+    eng.step_profile()  # discard warm-up spans
+    barrier()
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(dev.index if dev.index is not None else 0)
+    sampler.start()
+    stream = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = eng.run(vel, obs, profile=True)
+        launches += r.launches
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    step_ms, step_launches = eng.step_profile()
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    cu_batch = cell_updates_per_sample(p) * nsamples
+    value = args.steps * cu_batch * world / (ms_max / 1e3)
+    sgrad = args.steps * nsamples * world / (ms_max / 1e3)
+
+    # roofline of the time-step kernel
+    alg_total = algorithmic_bytes_per_sample(p) * nsamples * args.steps
+    achieved = alg_total / (step_ms / 1e3) / 1e9
+    peaks = {}
+    pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    avg_launch_ms = step_ms / max(step_launches, 1)
+    ninst = nsamples * p.ns
+    nres_avg = ninst * 2 * p.nt * args.steps / max(step_launches, 1)
+    traffic = load_traffic(p, nres_avg)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_src, "kernel": "k_step (fused FD step)",
+                "avg_launch_ms": avg_launch_ms, "step_share_of_region": step_ms / ms if ms else None,
+                "algorithmic_bytes_per_launch": alg_total / max(step_launches, 1)}
+
+    # plain comparator: one (sample, shot) per launch, shots in order, one sample
+    plain = None
+    if not args.no_plain:
+        peng = Fwi2dEngine(p, device=dev, graph=False, plain=True)
+        peng.run(vel[:1], obs)
+        torch.cuda.synchronize(dev)
+        q0 = torch.cuda.Event(enable_timing=True)
+        q1 = torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        peng.run(vel[:1], obs)
+        q1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = q0.elapsed_time(q1)
+        plain = {"sample_gradients_per_s": 1e3 / pms, "cell_updates_per_s": cell_updates_per_sample(p) / (pms / 1e3),
+                 "ms_per_sample": pms}
+        del peng
+        torch.cuda.empty_cache()
+
+    # end to end through the public Posterior.fwi: host float64 samples in, host loss/grad out
+    e2e = None
+    if not args.no_e2e:
+        import configparser
+        from geopvi_gb300.posterior import Posterior
+        cfg = configparser.ConfigParser()
+        cfg["FWI"] = {"nx": str(p.nx), "nz": str(p.nz), "pml": str(p.pml0), "Lc": str(p.Lc),
+                      "laplace_slover": "0", "ns": str(p.ns), "nt": str(p.nt), "ds": str(p.ds),
+                      "ns0": str(p.ns0), "depths": str(p.depths), "depthr": str(p.depthr), "nr": str(p.nr),
+                      "dr": str(p.dr), "nr0": str(p.nr0), "nt_interval": str(p.nt_interval), "dx": repr(p.dx),
+                      "dz": repr(p.dz), "dt": repr(p.dt), "f0": repr(p.f0)}
+        del eng
+        torch.cuda.empty_cache()
+        with tempfile.TemporaryDirectory() as td:
+            post = Posterior(obs.cpu().numpy(), cfg, sigma=1.0, paramfile=os.path.join(td, "p.txt"),
+                             device=dev, graph=False, hbm_budget=budget)
+            x = torch.from_numpy(w.samples.astype(np.float64))
+            loss, grad = post.fwi(x)  # warm-up (workspace allocation)
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                loss, grad = post.fwi(x)
+            t1 = time.perf_counter()
+            e2e_s = t1 - t0
+            tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+            if world > 1:
+                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_s = float(tt.item())
+            e2e = {"value": args.steps * cu_batch * world / e2e_s, "unit": "cell-updates/s",
+                   "h2d_bytes_per_step": int(x.numel() * 8), "d2h_bytes_per_step": int(loss.nbytes + grad.nbytes),
+                   "api": "geopvi_gb300.posterior.Posterior.fwi (host float64 in, numpy out)",
+                   "sample_gradients_per_s": args.steps * nsamples * world / e2e_s}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, kind, threads, desc = cpu_sample(p, w.samples[0], obs.cpu().numpy(), args.cpu_shots)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind, "sample": desc,
+               "seconds": dt, "sample_gradients_per_s": v / cell_updates_per_sample(p)}
+
+    if rank == 0:
+        out = {
+            "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)",
+            "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded models)",
+            "config": {"workload": WORKLOAD_NAMES[args.config], "samples": nsamples, "shots": p.ns,
+                       "grid": f"{p.nz}x{p.nx} (padded {p.ntz}x{p.ntx})", "nt": p.nt, "fd_order": 2 * p.Lc,
+                       "resident_solves": resident, "waves": -(-ninst // resident),
+                       "l2": "inputs larger than L2 (wavefield state of the resident solves >> 129 MB)",
+                       "parallelism": f"replicas x{world}"},
+            "sample_gradients_per_s": sgrad,
+            "plain": plain,
+            "batched_vs_plain": (sgrad / world) / plain["sample_gradients_per_s"] if plain else None,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

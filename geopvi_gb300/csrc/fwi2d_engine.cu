@@ -1,0 +1,753 @@
+// fwi2d_engine.cu -- host side of the GB300 acoustic FWI engine and its C ABI.
+//
+// Replaces the drivers fwi_2D / forward_2D (geopvi/forward/fwi2d/
+// fdtd2D_modelling.c:18-353, 356-675) and the per-sample loop of
+// Posterior.fwi (geopvi/forward/fwi2d/posterior.py:112-129).  The reference
+// runs shots one after another on the CPU, re-reads its parameter file and
+// re-allocates every buffer per sample; here every (sample, shot) solve of a
+// batch advances together, one fused kernel launch per time step, in a
+// caller-owned device workspace, optionally replayed from a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "../../include/geopvi_fwi2d.h"
+#include "fwi2d_kernels.cuh"
+
+namespace gbfwi {
+
+// ---------------------------------------------------------------------------
+// Parameter derivation (host)
+// ---------------------------------------------------------------------------
+
+// The reference's pi literal (fdtd2D_modelling.c:15).
+static const double kRefPi = 3.1415926;
+
+struct Derived {
+    Geom g;
+    std::vector<float> rik;   // Ricker wavelet per time step
+    std::vector<float> w;     // boundary weights
+    std::vector<double> omw;  // 1 - w, double
+};
+
+static int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// fd_coefficient (fdtd2D_modelling.c:1272-1326): double literals stored as float.
+static void fd_weights(int Lc, float *fd)
+{
+    for (int i = 0; i < 8; ++i) fd[i] = 0.0f;
+    switch (Lc) {
+    case 4:
+        fd[3] = (float)(1.0 / 90); fd[2] = (float)(-3.0 / 20); fd[1] = 1.5f;
+        fd[0] = (float)(-49.0 / 18);
+        break;
+    case 5:
+        fd[4] = (float)(-1.0 / 560); fd[3] = (float)(8.0 / 315); fd[2] = (float)(-1.0 / 5);
+        fd[1] = (float)(8.0 / 5); fd[0] = (float)(-205.0 / 72);
+        break;
+    case 6:
+        fd[5] = (float)(8.0 / 25200); fd[4] = (float)(-125.0 / 25200);
+        fd[3] = (float)(1000.0 / 25200); fd[2] = (float)(-6000.0 / 25200);
+        fd[1] = (float)(42000.0 / 25200); fd[0] = (float)(-73766.0 / 25200);
+        break;
+    case 7: {
+        const double den = 7.820582005659452e+44;
+        fd[6] = (float)(-4.702129633040854e+40 / den); fd[5] = (float)(8.12528000589218e+41 / den);
+        fd[4] = (float)(-6.982662505061379e+42 / den); fd[3] = (float)(4.13787407707198e+43 / den);
+        fd[2] = (float)(-2.0947987515168676e+44 / den);
+        fd[1] = (float)(1.3406712009703548e+45 / den);
+        fd[0] = (float)(-2.332705821577166e+45 / den);
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+// getrik (fdtd2D_modelling.c:1084-1093): the squared phase is held in a
+// float, the wavelet evaluated in double and stored as float.
+static void ricker(int nt, float dt, float f0, std::vector<float> &rik)
+{
+    rik.resize(nt);
+    for (int it = 0; it < nt; ++it) {
+        const float phase = (float)it * dt - 1.0f / f0;
+        const double arg = kRefPi * f0 * (double)phase;
+        const float a = (float)(arg * arg);
+        rik[it] = (float)((1.0 - 2.0 * a) * std::exp((double)(-a)));
+    }
+}
+
+static int validate(const gb_fwi2d_params &p)
+{
+    if (p.nx <= 0 || p.nz <= 0 || p.ns <= 0 || p.nt <= 0 || p.nr <= 0) return GB_FWI2D_EINVAL;
+    if (p.pml0 <= 0 || p.nt_interval <= 0) return GB_FWI2D_EINVAL;
+    if (!(p.dx > 0.0f) || !(p.dz > 0.0f) || !(p.dt > 0.0f) || !(p.f0 > 0.0f)) return GB_FWI2D_EINVAL;
+    if (p.laplace_solver == 1) return GB_FWI2D_ENOTSUP;  // pseudo-spectral Laplacian
+    if (p.laplace_solver != 0) return GB_FWI2D_EINVAL;
+    if (p.Lc < 3 || p.Lc > 6) return GB_FWI2D_EINVAL;     // fd_coefficient: Lc+1 in 4..7
+    if (p.nr > 1 && p.dr == 0) return GB_FWI2D_EINVAL;    // receivers would share one cell
+    const long long Lc = p.Lc + 1, pml = p.pml0 + Lc;
+    const long long ntz = p.nz + 2 * pml, ntx = p.nx + 2 * pml;
+    if (ntz > (1 << 20) || ntx > (1 << 20) || ntz * ntx > (1LL << 31)) return GB_FWI2D_EINVAL;
+    const long long s_iz = pml + p.depths, r_iz = pml + p.depthr;
+    if (s_iz < 0 || s_iz >= ntz || r_iz < 0 || r_iz >= ntz) return GB_FWI2D_EINVAL;
+    for (long long is : {0LL, (long long)p.ns - 1}) {
+        long long s_ix = is * p.ds + pml + p.ns0;
+        if (s_ix < 0 || s_ix >= ntx) return GB_FWI2D_EINVAL;
+    }
+    for (long long ir : {0LL, (long long)p.nr - 1}) {
+        long long r_ix = pml + ir * p.dr + p.nr0;
+        if (r_ix < 0 || r_ix >= ntx) return GB_FWI2D_EINVAL;
+    }
+    return GB_FWI2D_OK;
+}
+
+static int derive(const gb_fwi2d_params &p, Derived &d)
+{
+    int st = validate(p);
+    if (st) return st;
+    Geom &g = d.g;
+    std::memset(&g, 0, sizeof g);
+    g.Lc = p.Lc + 1;
+    g.pml = p.pml0 + g.Lc;
+    g.pml0 = p.pml0;
+    g.ntz = p.nz + 2 * g.pml;
+    g.ntx = p.nx + 2 * g.pml;
+    // Column offset so that the interior (ix = pml) starts on a 128-byte line.
+    g.xoff = (kTileX - g.pml % kTileX) % kTileX;
+    g.pitch = round_up(g.xoff + g.ntx, kTileX);
+    g.nx = p.nx;
+    g.nz = p.nz;
+    g.ipitch = round_up(p.nx, kTileX);
+    g.s_iz = g.pml + p.depths;
+    g.r_iz = g.pml + p.depthr;
+    g.r_ix0 = g.pml + p.nr0;
+    g.dr = p.dr;
+    g.nr = p.nr;
+    g.ds = p.ds;
+    g.s_ix0 = g.pml + p.ns0;
+    g.ns = p.ns;
+    g.nt = p.nt;
+    g.nti = p.nt_interval;
+    g.nt_save = p.nt / p.nt_interval + ((p.nt % p.nt_interval) ? 1 : 0);
+    g.tiles_x = g.pitch / kTileX;
+    g.tiles_z = (g.ntz + kTileZ - 1) / kTileZ;
+    g.fstride = (long long)g.ntz * g.pitch;
+    g.pstride = (long long)g.nz * g.ipitch;
+    g.dx = p.dx;
+    g.dz = p.dz;
+    g.dt = p.dt;
+    fd_weights(g.Lc, g.fd);
+    ricker(p.nt, p.dt, p.f0, d.rik);
+    d.w.resize(p.pml0);
+    d.omw.resize(p.pml0);
+    for (int i = 0; i < p.pml0; ++i) {
+        d.w[i] = (float)(1.0 - 1.0 * i / p.pml0);  // fdtd2D_modelling.c:229
+        d.omw[i] = 1.0 - (double)d.w[i];
+    }
+    return GB_FWI2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Workspace layout
+// ---------------------------------------------------------------------------
+
+struct Layout {
+    size_t vdt, ring, psave, gacc, syn, part, total;
+    int resident;
+};
+
+constexpr int kMisfitBlocks = 64;  // partial sums per sample for the misfit
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in_work,
+                          bool forward_only)
+{
+    Layout L{};
+    const long long ninst = (long long)nsamples * g.ns;
+    if (resident <= 0 || resident > ninst) resident = (int)ninst;
+    L.resident = resident;
+    size_t off = 0;
+    L.vdt = off;   off = align256(off + sizeof(float) * g.fstride * nsamples);
+    L.ring = off;  off = align256(off + sizeof(float) * g.fstride * 3 * resident);
+    L.psave = off;
+    if (!forward_only) off = align256(off + sizeof(float) * g.pstride * g.nt_save * resident);
+    L.gacc = off;
+    if (!forward_only) off = align256(off + sizeof(float) * g.pstride * ninst);
+    L.syn = off;
+    if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
+    L.part = off;  off = align256(off + sizeof(double) * kMisfitBlocks * nsamples);
+    L.total = off;
+    return L;
+}
+
+// ---------------------------------------------------------------------------
+// Auxiliary kernels
+// ---------------------------------------------------------------------------
+
+// Padded v*dt for every sample: get_velp's replication (a clamp) times dt,
+// the float product that powf(v*dt, 2) and s = v*dt/dx start from.
+__global__ void k_prepare(const Geom g, const float *__restrict__ vel, float *__restrict__ vdt,
+                          int nsamples)
+{
+    const long long total = (long long)nsamples * g.fstride;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(e / g.fstride);
+        const long long r = e - (long long)s * g.fstride;
+        const int iz = (int)(r / g.pitch);
+        const int ix = (int)(r - (long long)iz * g.pitch) - g.xoff;
+        float v = 0.0f;
+        if (ix >= 0 && ix < g.ntx)
+            v = fm(padded_velocity(g, vel + (long long)s * g.nx * g.nz, iz, ix), g.dt);
+        vdt[e] = v;
+    }
+}
+
+// grad[s][cell] = sum over shots, in double, of the per-shot accumulated
+// sum(psave * p2), times the reference's per-term factor
+// -2/powf(v,3) * nt_interval * dt (FWI) or nt_interval * dt (imaging).
+__global__ void k_reduce_grad(const Geom g, const float *__restrict__ gacc,
+                              const float *__restrict__ vel, float *__restrict__ grad,
+                              int nsamples, int imaging)
+{
+    const long long cells = (long long)g.nz * g.nx;
+    const long long total = (long long)nsamples * cells;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(e / cells);
+        const long long k = e - (long long)s * cells;
+        const int iz = (int)(k / g.nx), ix = (int)(k - (long long)iz * g.nx);
+        const long long pc = (long long)iz * g.ipitch + ix;
+        double acc = 0.0;
+        for (int shot = 0; shot < g.ns; ++shot)
+            acc += (double)gacc[((long long)s * g.ns + shot) * g.pstride + pc];
+        double coef = (double)g.nti * (double)g.dt;
+        if (!imaging) {
+            const double v = (double)vel[e];
+            const float v3 = __double2float_rn(v * v * v);  // powf(v, 3) as a rounded float
+            coef = (-2.0 / (double)v3) * coef;
+        }
+        grad[e] = __double2float_rn(coef * acc);
+    }
+}
+
+// Misfit 0.5*sum((syn-obs)^2) per sample: float residual as the reference
+// forms it (record -= obs), squares summed in double.  Two fixed-order
+// passes keep the result deterministic.
+__global__ void k_misfit_partial(const float *__restrict__ syn, const float *__restrict__ obs,
+                                 long long per_sample, double *__restrict__ part)
+{
+    const int s = blockIdx.y;
+    const float *sy = syn + (long long)s * per_sample;
+    double acc = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per_sample;
+         e += (long long)gridDim.x * blockDim.x) {
+        const float r = fs(sy[e], obs[e]);
+        acc += (double)r * (double)r;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double warp_sums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_sums[wid] = acc;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        acc = lane < nw ? warp_sums[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) part[(long long)s * gridDim.x + blockIdx.x] = acc;
+    }
+}
+
+__global__ void k_misfit_final(const double *__restrict__ part, double *__restrict__ misfit,
+                               int nsamples)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsamples) return;
+    double acc = 0.0;
+    for (int i = 0; i < kMisfitBlocks; ++i) acc += part[(long long)s * kMisfitBlocks + i];
+    misfit[s] = 0.5 * acc;
+}
+
+// ---------------------------------------------------------------------------
+// Cached per-device tables and graphs
+// ---------------------------------------------------------------------------
+
+struct DeviceTables {
+    float *w = nullptr;
+    double *omw = nullptr;
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+};
+
+static std::mutex g_mutex;
+static std::map<std::pair<int, int>, DeviceTables> g_tables;  // (device, pml0)
+static std::map<std::vector<long long>, GraphEntry> g_graphs;
+static thread_local long long t_last_launches = 0;
+
+// Event pairs around the step-kernel loops of profiled calls, accumulated
+// until gb_fwi2d_profile_step_ms reads (and clears) them.
+struct StepProfile {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans;
+    long long launches = 0;
+    void reset()
+    {
+        for (auto &e : spans) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+        spans.clear();
+        launches = 0;
+    }
+};
+static thread_local StepProfile t_profile;
+
+static int get_tables(const Derived &d, DeviceTables &out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    auto key = std::make_pair(dev, d.g.pml0);
+    auto it = g_tables.find(key);
+    if (it != g_tables.end()) {
+        out = it->second;
+        return GB_FWI2D_OK;
+    }
+    DeviceTables t;
+    if (cudaMalloc(&t.w, sizeof(float) * d.w.size()) != cudaSuccess) return GB_FWI2D_ENOMEM;
+    if (cudaMalloc(&t.omw, sizeof(double) * d.omw.size()) != cudaSuccess) {
+        cudaFree(t.w);
+        return GB_FWI2D_ENOMEM;
+    }
+    if (cudaMemcpy(t.w, d.w.data(), sizeof(float) * d.w.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(t.omw, d.omw.data(), sizeof(double) * d.omw.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        cudaFree(t.w);
+        cudaFree(t.omw);
+        return GB_FWI2D_ECUDA;
+    }
+    g_tables[key] = t;
+    out = t;
+    return GB_FWI2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch sequence
+// ---------------------------------------------------------------------------
+
+template <int H>
+static void launch_step(bool adj, const Geom &g, const Batch &b, int nres, int k, int it,
+                        float rik_it, cudaStream_t st)
+{
+    dim3 grid(g.tiles_x * g.tiles_z, nres), block(kTileX, kBlockZ);
+    if (adj)
+        k_step<H, true><<<grid, block, 0, st>>>(g, b, k, it, rik_it);
+    else
+        k_step<H, false><<<grid, block, 0, st>>>(g, b, k, it, rik_it);
+}
+
+static void step(bool adj, const Geom &g, const Batch &b, int nres, int k, int it, float rik_it,
+                 cudaStream_t st)
+{
+    switch (g.Lc - 1) {
+    case 3: launch_step<3>(adj, g, b, nres, k, it, rik_it, st); break;
+    case 4: launch_step<4>(adj, g, b, nres, k, it, rik_it, st); break;
+    case 5: launch_step<5>(adj, g, b, nres, k, it, rik_it, st); break;
+    default: launch_step<6>(adj, g, b, nres, k, it, rik_it, st); break;
+    }
+}
+
+struct Call {
+    const Derived *d;
+    DeviceTables tab;
+    Layout L;
+    int nsamples;
+    const float *vel, *obs;
+    float *syn, *grad;
+    double *misfit;
+    unsigned flags;
+    char *work;
+    bool profile;
+};
+
+static int grid_for(long long n, int threads)
+{
+    long long b = (n + threads - 1) / threads;
+    return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
+}
+
+// Enqueue the whole batch on `st`; returns the number of kernel launches.
+static long long enqueue(const Call &c, cudaStream_t st)
+{
+    const Geom &g = c.d->g;
+    long long launches = 0;
+    float *vdt = (float *)(c.work + c.L.vdt);
+    float *ring = (float *)(c.work + c.L.ring);
+    float *gacc = (float *)(c.work + c.L.gacc);
+    float *syn = c.syn ? c.syn : (float *)(c.work + c.L.syn);
+    double *part = (double *)(c.work + c.L.part);
+    const bool imaging = (c.flags & GB_FWI2D_IMAGING) != 0;
+    const bool plain = (c.flags & GB_FWI2D_PLAIN) != 0;
+    const bool fwd_only = (c.flags & GB_FWI2D_FORWARD_ONLY) != 0;
+    const long long ninst = (long long)c.nsamples * g.ns;
+
+    k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt,
+                                                                                c.nsamples);
+    ++launches;
+    if (!fwd_only) cudaMemsetAsync(gacc, 0, sizeof(float) * g.pstride * ninst, st);
+
+    Batch b;
+    b.vdt = vdt;
+    b.vel = c.vel;
+    b.obs = c.obs;
+    b.syn = syn;
+    b.ring = ring;
+    b.psave = (float *)(c.work + c.L.psave);
+    b.gacc = gacc;
+    b.wtab = c.tab.w;
+    b.omw = c.tab.omw;
+    b.imaging = imaging ? 1 : 0;
+    b.store = fwd_only ? 0 : 1;
+
+    const int wave = plain ? 1 : c.L.resident;
+    for (long long i0 = 0; i0 < ninst; i0 += wave) {
+        const int nres = (int)std::min<long long>(wave, ninst - i0);
+        b.inst0 = (int)i0;
+        for (int pass = 0; pass < (fwd_only ? 1 : 2); ++pass) {
+            const bool adj = pass == 1;
+            // p0 and p1 of step 0 start at zero (wavefield_initialization).
+            cudaMemset2DAsync(ring, sizeof(float) * 3 * g.fstride, 0, sizeof(float) * 2 * g.fstride,
+                              nres, st);
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (c.profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
+                cudaEventRecord(e0, st);
+            for (int k = 0; k < g.nt; ++k) {
+                const int it = adj ? g.nt - 1 - k : k;
+                step(adj, g, b, nres, k, it, adj ? 0.0f : c.d->rik[it], st);
+                ++launches;
+            }
+            if (e1) {
+                cudaEventRecord(e1, st);
+                t_profile.spans.emplace_back(e0, e1);
+                t_profile.launches += g.nt;
+            }
+        }
+    }
+    if (c.grad && !fwd_only) {
+        k_reduce_grad<<<grid_for((long long)c.nsamples * g.nz * g.nx, 256), 256, 0, st>>>(
+            g, gacc, c.vel, c.grad, c.nsamples, imaging ? 1 : 0);
+        ++launches;
+    }
+    if (c.misfit) {
+        k_misfit_partial<<<dim3(kMisfitBlocks, c.nsamples), 256, 0, st>>>(
+            syn, c.obs, (long long)g.ns * g.nt * g.nr, part);
+        k_misfit_final<<<(c.nsamples + 127) / 128, 128, 0, st>>>(part, c.misfit, c.nsamples);
+        launches += 2;
+    }
+    return launches;
+}
+
+static std::vector<long long> graph_key(const Call &c, int dev)
+{
+    const Geom &g = c.d->g;
+    std::vector<long long> k;
+    k.push_back(dev);
+    const int *gi = (const int *)&g;
+    for (size_t i = 0; i < sizeof(Geom) / sizeof(int); ++i) k.push_back(gi[i]);
+    k.push_back(c.nsamples);
+    k.push_back((long long)(uintptr_t)c.vel);
+    k.push_back((long long)(uintptr_t)c.obs);
+    k.push_back((long long)(uintptr_t)c.syn);
+    k.push_back((long long)(uintptr_t)c.grad);
+    k.push_back((long long)(uintptr_t)c.misfit);
+    k.push_back((long long)(uintptr_t)c.work);
+    k.push_back(c.flags);
+    k.push_back(c.L.resident);
+    // The Ricker table depends on f0, which Geom does not hold.
+    for (float r : {c.d->rik.empty() ? 0.0f : c.d->rik[0], c.d->rik.size() > 1 ? c.d->rik[1] : 0.0f}) {
+        int bits;
+        std::memcpy(&bits, &r, sizeof bits);
+        k.push_back(bits);
+    }
+    return k;
+}
+
+static int run_graph(const Call &c, cudaStream_t st, long long &launches)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    std::vector<long long> key = graph_key(c, dev);
+    {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) {
+            launches = it->second.launches;
+            return cudaGraphLaunch(it->second.exec, st) == cudaSuccess ? GB_FWI2D_OK
+                                                                      : GB_FWI2D_ECUDA;
+        }
+    }
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return GB_FWI2D_ECUDA;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaStreamDestroy(cap);
+        return GB_FWI2D_ECUDA;
+    }
+    long long n = enqueue(c, cap);
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return GB_FWI2D_ECUDA;
+    GraphEntry ge;
+    e = cudaGraphInstantiate(&ge.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return GB_FWI2D_ECUDA;
+    ge.launches = n;
+    {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        g_graphs[key] = ge;
+    }
+    launches = n;
+    return cudaGraphLaunch(ge.exec, st) == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
+}
+
+}  // namespace gbfwi
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace gbfwi;
+
+namespace {
+
+bool read_line_value(FILE *fp, const char *fmt, void *dst)
+{
+    char line[256];
+    if (!std::fgets(line, sizeof line, fp)) return false;
+    if (std::fscanf(fp, "\n") < 0) { /* only whitespace skipped */ }
+    if (std::fscanf(fp, fmt, dst) != 1) return false;
+    if (std::fscanf(fp, "\n") < 0) { /* end of file after the last value */ }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gb_fwi2d_version(void) { return "geopvi_gb300 fwi2d 0.1 (sm_103a)"; }
+
+int gb_fwi2d_read_params(const char *path, gb_fwi2d_params *out)
+{
+    if (!path || !out) return GB_FWI2D_EINVAL;
+    FILE *fp = std::fopen(path, "r");
+    if (!fp) return GB_FWI2D_ENOENT;
+    gb_fwi2d_params p;
+    int *ints[] = {&p.nx, &p.nz, &p.pml0, &p.Lc, &p.laplace_solver, &p.ns, &p.nt, &p.ds,
+                   &p.ns0, &p.depths, &p.depthr, &p.nr, &p.dr, &p.nr0, &p.nt_interval};
+    float *floats[] = {&p.dx, &p.dz, &p.dt, &p.f0};
+    bool ok = true;
+    for (int *v : ints) ok = ok && read_line_value(fp, "%d", v);
+    for (float *v : floats) ok = ok && read_line_value(fp, "%f", v);
+    std::fclose(fp);
+    if (!ok) return GB_FWI2D_EINVAL;
+    *out = p;
+    return GB_FWI2D_OK;
+}
+
+int gb_fwi2d_validate(const gb_fwi2d_params *p)
+{
+    if (!p) return GB_FWI2D_EINVAL;
+    return validate(*p);
+}
+
+size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_resident,
+                                unsigned flags)
+{
+    (void)flags;
+    if (!p || nsamples <= 0) return 0;
+    Derived d;
+    if (derive(*p, d)) return 0;
+    return plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0).total;
+}
+
+int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
+                   float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
+                   void *work, size_t work_bytes, void *stream)
+{
+    t_last_launches = 0;
+    if (!p || nsamples <= 0 || !vel || !obs || !work) return GB_FWI2D_EINVAL;
+    if (flags & GB_FWI2D_CHECKPOINT) return GB_FWI2D_ENOTSUP;
+    Derived d;
+    int st = derive(*p, d);
+    if (st) return st;
+    Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0);
+    if (work_bytes < L.total) return GB_FWI2D_ENOMEM;
+    Call c;
+    c.d = &d;
+    c.L = L;
+    c.nsamples = nsamples;
+    c.vel = vel;
+    c.obs = obs;
+    c.syn = syn;
+    c.grad = grad;
+    c.misfit = misfit;
+    c.flags = flags;
+    c.work = (char *)work;
+    c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
+    st = get_tables(d, c.tab);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    long long launches = 0;
+    if (flags & GB_FWI2D_GRAPH) {
+        st = run_graph(c, s, launches);
+    } else {
+        launches = enqueue(c, s);
+        st = cudaGetLastError() == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
+    }
+    t_last_launches = launches;
+    return st;
+}
+
+long long gb_fwi2d_last_launch_count(void) { return t_last_launches; }
+
+double gb_fwi2d_profile_step_ms(long long *launches)
+{
+    if (launches) *launches = t_profile.launches;
+    if (t_profile.spans.empty()) return -1.0;
+    double total = 0.0;
+    for (auto &e : t_profile.spans) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e.second) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e.first, e.second) != cudaSuccess) {
+            t_profile.reset();
+            return -1.0;
+        }
+        total += ms;
+    }
+    t_profile.reset();
+    return total;
+}
+
+void gb_fwi2d_release_caches(void)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    for (auto &kv : g_graphs) cudaGraphExecDestroy(kv.second.exec);
+    g_graphs.clear();
+    for (auto &kv : g_tables) {
+        cudaFree(kv.second.w);
+        cudaFree(kv.second.omw);
+    }
+    g_tables.clear();
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Host-buffer drop-ins for fwi_2D / forward_2D
+// ---------------------------------------------------------------------------
+namespace {
+
+struct HostCallBuffers {
+    int dev = -1;
+    size_t bytes = 0;
+    char *base = nullptr;
+    cudaStream_t stream = nullptr;
+};
+std::mutex g_host_mutex;
+HostCallBuffers g_host;
+
+int host_run(const char *input_file, const float *vel_inner, float *record_syn,
+             const float *record_obs, float *grad, int run_fwi, int verbose, bool with_grad)
+{
+    if (!input_file || !vel_inner || !record_syn) return GB_FWI2D_EINVAL;
+    gb_fwi2d_params p;
+    int st = gb_fwi2d_read_params(input_file, &p);
+    if (st) {
+        if (verbose) std::printf("Cannot open %s!\n", input_file);
+        return st;
+    }
+    Derived d;
+    st = derive(p, d);
+    if (st) return st;
+    const size_t ncell = (size_t)p.nx * p.nz;
+    for (size_t i = 0; i < ncell; ++i)
+        if (std::isnan(vel_inner[i])) return GB_FWI2D_ENAN;
+    const size_t ndata = (size_t)p.ns * p.nt * p.nr;
+    Layout L = plan_layout(d.g, 1, 0, true, !with_grad);
+    const size_t o_vel = 0, o_obs = align256(sizeof(float) * ncell);
+    const size_t o_syn = align256(o_obs + sizeof(float) * ndata);
+    const size_t o_grad = align256(o_syn + sizeof(float) * ndata);
+    const size_t o_work = align256(o_grad + sizeof(float) * ncell);
+    const size_t need = o_work + L.total;
+
+    std::lock_guard<std::mutex> lk(g_host_mutex);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    if (g_host.dev != dev || g_host.bytes < need) {
+        if (g_host.base) cudaFree(g_host.base);
+        if (g_host.stream && g_host.dev != dev) {
+            cudaStreamDestroy(g_host.stream);
+            g_host.stream = nullptr;
+        }
+        g_host.base = nullptr;
+        g_host.bytes = 0;
+        if (cudaMalloc(&g_host.base, need) != cudaSuccess) return GB_FWI2D_ENOMEM;
+        g_host.bytes = need;
+        g_host.dev = dev;
+    }
+    if (!g_host.stream && cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking) != cudaSuccess)
+        return GB_FWI2D_ECUDA;
+    cudaStream_t s = g_host.stream;
+    char *b = g_host.base;
+    if (verbose) {
+        std::printf("ntx=%d, ntz=%d\n", d.g.ntx, d.g.ntz);
+        std::printf("nx=%d,  nz=%d,  nt=%d,  ns=%d\n", p.nx, p.nz, p.nt, p.ns);
+    }
+    cudaMemcpyAsync(b + o_vel, vel_inner, sizeof(float) * ncell, cudaMemcpyHostToDevice, s);
+    if (with_grad)
+        cudaMemcpyAsync(b + o_obs, record_obs, sizeof(float) * ndata, cudaMemcpyHostToDevice, s);
+    else
+        cudaMemsetAsync(b + o_obs, 0, sizeof(float) * ndata, s);
+    unsigned flags = (run_fwi ? 0u : GB_FWI2D_IMAGING) | (with_grad ? 0u : GB_FWI2D_FORWARD_ONLY);
+    st = gb_fwi2d_batch(&p, 1, (const float *)(b + o_vel), (const float *)(b + o_obs),
+                        (float *)(b + o_syn), with_grad ? (float *)(b + o_grad) : nullptr, nullptr,
+                        flags, 0, b + o_work, L.total, s);
+    if (st) return st;
+    std::vector<float> g(with_grad ? ncell : 0);
+    cudaMemcpyAsync(record_syn, b + o_syn, sizeof(float) * ndata, cudaMemcpyDeviceToHost, s);
+    if (with_grad) cudaMemcpyAsync(g.data(), b + o_grad, sizeof(float) * ncell, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GB_FWI2D_ECUDA;
+    if (with_grad)
+        for (size_t i = 0; i < ncell; ++i) grad[i] += g[i];  // the reference accumulates into grad
+    return GB_FWI2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fwi_2D(char input_file[200], float *vel_inner, float *record_syn, float *record_obs,
+           float *grad, int run_fwi, int verbose)
+{
+    if (!record_obs || !grad) return GB_FWI2D_EINVAL;
+    return host_run(input_file, vel_inner, record_syn, record_obs, grad, run_fwi, verbose, true);
+}
+
+int forward_2D(char input_file[200], float *vel_inner, float *record_syn, int run_fwi, int verbose)
+{
+    (void)run_fwi;  // forward_2D stores the field either way; only the data are returned
+    return host_run(input_file, vel_inner, record_syn, nullptr, nullptr, 1, verbose, false);
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+"""Batched GPU solves through the C ABI, with torch for device memory and streams.
+
+``Fwi2dEngine.run`` takes a batch of velocity models already on the GPU and
+returns per-sample misfits and gradients (and optionally the synthetic data),
+all as CUDA tensors.  It replaces the per-sample ``aco2d.fwi`` loop of
+``Posterior.fwi`` (geopvi/forward/fwi2d/posterior.py:112-129) with one
+enqueue of every (sample, shot) solve.  The workspace is allocated once per
+batch shape and reused; with ``graph=True`` the whole step sequence is
+captured once and replayed from a CUDA graph on later calls.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import torch
+
+from . import _native
+from .params import Params
+
+
+@dataclass
+class RunResult:
+    misfit: torch.Tensor          # (n,) float64
+    grad: torch.Tensor | None     # (n, nz*nx) float32
+    syn: torch.Tensor | None      # (n, ns*nt*nr) float32
+    launches: int                 # kernel launches enqueued by the call
+
+
+def _require_cuda(t: torch.Tensor, name: str, dtype: torch.dtype) -> None:
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+class Fwi2dEngine:
+    """One solver configuration bound to one CUDA device.
+
+    max_resident: (sample, shot) solves whose wavefield state is held at once;
+        None sizes it from ``hbm_budget`` (bytes, default 60% of free memory).
+    graph: capture the step sequence in a CUDA graph on first use and replay.
+    plain: one solve per launch, shots in order -- the comparator form.
+    """
+
+    def __init__(self, params: Params, device=None, max_resident: int | None = None,
+                 hbm_budget: int | None = None, graph: bool = True, plain: bool = False):
+        self.params = params
+        self.lib = _native.load()
+        self.device = torch.device(device if device is not None else "cuda")
+        if self.device.type != "cuda":
+            raise ValueError("the engine runs on CUDA devices only")
+        if not torch.cuda.is_available():
+            raise RuntimeError("no CUDA device: the GB300 engine has no CPU path")
+        params.validate()
+        self.max_resident = max_resident
+        self.hbm_budget = hbm_budget
+        self.graph = graph
+        self.plain = plain
+        self._cp = params.c()
+        self._work: torch.Tensor | None = None
+        self._work_key = None
+        self._outs = {}
+
+    # ---- sizing ----
+    def workspace_bytes(self, nsamples: int, resident: int, flags: int = 0) -> int:
+        return int(self.lib.gb_fwi2d_workspace_bytes(ctypes.byref(self._cp), nsamples, resident, flags))
+
+    def per_solve_bytes(self) -> int:
+        return self.workspace_bytes(1, 1) if self.params.ns == 1 else \
+            self.workspace_bytes(1, 2) - self.workspace_bytes(1, 1)
+
+    def resident_for(self, nsamples: int, flags: int = 0) -> int:
+        ninst = nsamples * self.params.ns
+        if self.max_resident:
+            return max(1, min(self.max_resident, ninst))
+        if flags & _native.FLAG_PLAIN:
+            return 1
+        budget = self.hbm_budget
+        if budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            budget = int(free * 0.6)
+        base = self.workspace_bytes(nsamples, 1, flags)
+        per = max(1, self.workspace_bytes(nsamples, 2, flags) - base) if ninst > 1 else 1
+        fit = 1 + max(0, (budget - base) // per)
+        return int(max(1, min(ninst, fit)))
+
+    def _workspace(self, nsamples: int, flags: int) -> tuple[torch.Tensor, int]:
+        resident = self.resident_for(nsamples, flags)
+        key = (nsamples, resident, flags & (_native.FLAG_FORWARD_ONLY | _native.FLAG_CHECKPOINT))
+        if self._work_key != key:
+            nbytes = self.workspace_bytes(nsamples, resident, flags)
+            if nbytes == 0:
+                raise _native.EngineError(_native.EINVAL, "gb_fwi2d_workspace_bytes")
+            self._work = None
+            torch.cuda.empty_cache() if torch.cuda.is_initialized() else None
+            self._work = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._work_key = key
+        return self._work, resident
+
+    # ---- solve ----
+    def run(self, vel: torch.Tensor, obs: torch.Tensor, *, imaging: bool = False,
+            want_grad: bool = True, want_syn: bool = False, forward_only: bool = False,
+            profile: bool = False, out: dict | None = None) -> RunResult:
+        """vel (n, nz*nx) float32 CUDA; obs (ns*nt*nr,) float32 CUDA.
+
+        Returns misfit (n,) float64, grad (n, nz*nx) float32 in the reference's
+        scaling (the array fwi_2D accumulates), syn (n, ns*nt*nr) if asked.
+        Outputs are reused across calls of the same shape unless ``out`` is given.
+        """
+        p = self.params
+        if vel.dim() == 1:
+            vel = vel.unsqueeze(0)
+        _require_cuda(vel, "vel", torch.float32)
+        _require_cuda(obs, "obs", torch.float32)
+        n = vel.shape[0]
+        if vel.shape[1] != p.ncell:
+            raise ValueError(f"vel has {vel.shape[1]} cells per model, expected nz*nx = {p.ncell}")
+        if obs.numel() != p.data_len:
+            raise ValueError(f"obs has {obs.numel()} values, expected ns*nt*nr = {p.data_len}")
+        flags = 0
+        if imaging:
+            flags |= _native.FLAG_IMAGING
+        if self.plain:
+            flags |= _native.FLAG_PLAIN
+        if profile:
+            flags |= _native.FLAG_PROFILE
+        elif self.graph and not self.plain:
+            flags |= _native.FLAG_GRAPH
+        if forward_only:
+            flags |= _native.FLAG_FORWARD_ONLY
+            want_grad = False
+            want_syn = True
+        work, resident = self._workspace(n, flags)
+        bufs = out if out is not None else self._outs.setdefault((n, want_grad, want_syn), {})
+        if "misfit" not in bufs:
+            bufs["misfit"] = torch.empty(n, dtype=torch.float64, device=self.device)
+        if want_grad and "grad" not in bufs:
+            bufs["grad"] = torch.empty(n, p.ncell, dtype=torch.float32, device=self.device)
+        if want_syn and "syn" not in bufs:
+            bufs["syn"] = torch.empty(n, p.data_len, dtype=torch.float32, device=self.device)
+        misfit = bufs["misfit"]
+        grad = bufs.get("grad") if want_grad else None
+        syn = bufs.get("syn") if want_syn else None
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        with torch.cuda.device(self.device):
+            st = self.lib.gb_fwi2d_batch(
+                ctypes.byref(self._cp), n, vel.data_ptr(), obs.data_ptr(),
+                syn.data_ptr() if syn is not None else None,
+                grad.data_ptr() if grad is not None else None,
+                misfit.data_ptr(), flags, resident, work.data_ptr(), work.numel(), stream)
+        _native.check(st, "gb_fwi2d_batch")
+        return RunResult(misfit=misfit, grad=grad, syn=syn,
+                         launches=int(self.lib.gb_fwi2d_last_launch_count()))
+
+    def step_profile(self) -> tuple[float, int]:
+        """(device ms, launches) of the time-step kernels of every
+        ``run(..., profile=True)`` on this thread since the previous read."""
+        n = ctypes.c_longlong(0)
+        ms = float(self.lib.gb_fwi2d_profile_step_ms(ctypes.byref(n)))
+        if ms < 0:
+            raise RuntimeError("no profiled run since the last read")
+        return ms, int(n.value)

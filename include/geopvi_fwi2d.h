@@ -1,0 +1,121 @@
+/*
+ * geopvi_fwi2d.h -- C ABI of the GB300 acoustic FWI engine.
+ *
+ * Drop-in boundary for GeoPVI's geopvi/forward/fwi2d solver.  The entry
+ * points fall in three groups:
+ *
+ *  1. Exact replacements of the reference's C entry points that the Cython
+ *     module `aco2d` binds (geopvi/forward/fwi2d/pyacofwi2D.h:2-3,
+ *     pyacofwi2D.pyx:4-6): `fwi_2D` and `forward_2D`, same names, same
+ *     argument meaning, host buffers, parameters read from the positional
+ *     text file.  They return a status instead of calling exit().
+ *  2. The parameter reader (read_parameters, fdtd2D_modelling.c:1328-1379)
+ *     as a typed struct, so callers can skip the text file.
+ *  3. The batched device API: every (sample, shot) solve of a batch runs on
+ *     one GPU, stream-ordered, in caller-owned device buffers.  It replaces
+ *     the per-sample loop of Posterior.fwi / Posterior.fwi_parallel
+ *     (geopvi/forward/fwi2d/posterior.py:112-149).
+ *
+ * Plain pointers and sizes only; `stream` is a cudaStream_t passed as void*.
+ * No entry point exits or aborts; all return GB_FWI2D_OK (0) or a negative
+ * status code.
+ */
+#ifndef GEOPVI_FWI2D_H
+#define GEOPVI_FWI2D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define GB_FWI2D_OK 0
+#define GB_FWI2D_ENOENT (-2)     /* parameter file missing */
+#define GB_FWI2D_ENOMEM (-12)    /* device memory / workspace too small */
+#define GB_FWI2D_EINVAL (-22)    /* bad geometry, sizes or pointers */
+#define GB_FWI2D_ENOTSUP (-95)   /* valid in the reference but not built here */
+#define GB_FWI2D_ENAN (-1001)    /* NaN/Inf in the velocity input */
+#define GB_FWI2D_ECUDA (-1002)   /* a CUDA runtime call failed */
+
+/* Solver parameters, in the order and with the types read_parameters uses
+ * (fdtd2D_modelling.c:1328-1356; file layout written by
+ * prepare_fwi_parameters, posterior.py:27-68).  Lc is the value in the file
+ * (the half-order); the solver uses Lc+1 internally (fdtd2D_modelling.c:70). */
+typedef struct gb_fwi2d_params {
+    int nx, nz, pml0, Lc, laplace_solver, ns, nt, ds, ns0, depths, depthr, nr, dr, nr0,
+        nt_interval;
+    float dx, dz, dt, f0;
+} gb_fwi2d_params;
+
+/* Flags for gb_fwi2d_batch. */
+#define GB_FWI2D_IMAGING 0x1u    /* run_fwi = 0: zero-lag imaging (record = obs, psave = p) */
+#define GB_FWI2D_PLAIN 0x2u      /* one (sample, shot) per launch, shots in order (comparator) */
+#define GB_FWI2D_GRAPH 0x4u      /* capture the step sequence once in a CUDA graph, replay after */
+#define GB_FWI2D_CHECKPOINT 0x8u /* store sqrt(nt) checkpoints, recompute the forward in segments */
+#define GB_FWI2D_FORWARD_ONLY 0x10u /* synthetic data only (forward_2D): no adjoint, no stored field */
+#define GB_FWI2D_PROFILE 0x20u   /* time the step-kernel loops with CUDA events (not with GRAPH) */
+
+/* read_parameters (fdtd2D_modelling.c:1328): parse the positional file. */
+int gb_fwi2d_read_params(const char *path, gb_fwi2d_params *out);
+
+/* Check a parameter set the way the solver needs it (grid, geometry inside
+ * the padded grid, FD order, time sampling).  GB_FWI2D_OK or EINVAL/ENOTSUP. */
+int gb_fwi2d_validate(const gb_fwi2d_params *p);
+
+/* Drop-in for fwi_2D (fdtd2D_modelling.c:18-353, bound at pyacofwi2D.pyx:4).
+ * Host buffers: vel_inner[nz*nx], record_obs[ns*nt*nr] (shot, time, receiver),
+ * record_syn[ns*nt*nr] written, grad[nz*nx] ACCUMULATED (+=) as in the
+ * reference.  run_fwi = 1: misfit gradient; 0: imaging condition. */
+int fwi_2D(char input_file[200], float *vel_inner, float *record_syn, float *record_obs,
+           float *grad, int run_fwi, int verbose);
+
+/* Drop-in for forward_2D (fdtd2D_modelling.c:356-675, bound at pyacofwi2D.pyx:5):
+ * synthetic data only, record_syn[ns*nt*nr]. */
+int forward_2D(char input_file[200], float *vel_inner, float *record_syn, int run_fwi, int verbose);
+
+/* Device-memory bytes gb_fwi2d_batch needs for `nsamples` models when at
+ * most `max_resident` (sample, shot) solves hold their wavefield state at
+ * once (0 = all of them).  The state of one solve is three padded wavefields,
+ * the stored forward wavefield (or its checkpoints) and a gradient
+ * accumulator; the batch runs in ceil(nsamples*ns / max_resident) waves. */
+size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_resident,
+                                unsigned flags);
+
+/* Batched misfit + gradient on the device (replaces the sample loop of
+ * Posterior.fwi, posterior.py:112-129, and the per-sample aco2d.fwi call,
+ * pyacofwi2D.pyx:11-30).  Device pointers:
+ *   vel    [nsamples][nz*nx]       velocity models (float32)
+ *   obs    [ns][nt][nr]            observed data, shared by all samples
+ *   syn    [nsamples][ns][nt][nr]  synthetic data out (may be NULL: kept in workspace)
+ *   grad   [nsamples][nz*nx]       gradient out (overwritten, reference scaling)
+ *   misfit [nsamples]              0.5*sum((syn-obs)^2) out, FP64 (may be NULL)
+ * work/work_bytes: device workspace of at least
+ * gb_fwi2d_workspace_bytes(p, nsamples, max_resident, flags).
+ * Stream-ordered on `stream`; returns after enqueueing all work. */
+int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
+                   float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
+                   void *work, size_t work_bytes, void *stream);
+
+/* Number of kernel launches the last gb_fwi2d_batch call on this thread
+ * enqueued (graph replays count the kernels inside the graph). */
+long long gb_fwi2d_last_launch_count(void);
+
+/* gb_fwi2d_batch calls made with GB_FWI2D_PROFILE on this thread wrap each
+ * pass's run of time-step kernels in a pair of CUDA events.  This waits for
+ * the events recorded since the previous read, returns the summed device time
+ * of those step kernels in milliseconds (negative if there were none) and in
+ * *launches the number of step-kernel launches covered, then clears them. */
+double gb_fwi2d_profile_step_ms(long long *launches);
+
+/* Release cached device tables and CUDA graphs held by the library. */
+void gb_fwi2d_release_caches(void);
+
+/* Library version string. */
+const char *gb_fwi2d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEOPVI_FWI2D_H */

@@ -1,0 +1,132 @@
+"""C ABI and host-side logic, no GPU needed.
+
+The library loads without a device; only the host-side entry points
+(parameter file, validation, workspace sizing) are called here.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cases
+from geopvi_gb300 import _native
+from geopvi_gb300.params import Params, prepare_fwi_parameters, read_paramfile, write_paramfile
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "geopvi_fwi2d.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", text)))
+
+
+def test_header_lists_every_export():
+    assert set(declared_functions()) == set(_native.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    for name in declared_functions():
+        assert hasattr(engine_lib, name), f"{name} not exported"
+    assert b"sm_103a" in engine_lib.gb_fwi2d_version()
+
+
+def test_read_params_matches_writer(engine_lib, tmp_path):
+    for c in cases.SMALL.values():
+        p = c["params"]
+        path = str(tmp_path / "input_param.txt")
+        write_paramfile(path, p)
+        back = read_paramfile(path)
+        for f in _native.INT_FIELDS:
+            assert getattr(back, f) == getattr(p, f)
+        for f in _native.FLOAT_FIELDS:
+            assert np.float32(getattr(back, f)) == np.float32(getattr(p, f))
+
+
+def test_prepare_fwi_parameters_layout(engine_lib, tmp_path):
+    """The INI -> positional file of posterior.py:27-68, read back by the C reader."""
+    import configparser
+    cfg = configparser.ConfigParser()
+    cfg.read_string("""[FWI]
+nx = 250
+nz = 110
+layer_fixed = 10
+vel_fixed = 1950
+pml = 10
+Lc = 3
+laplace_slover = 0
+ns = 12
+nt = 2001
+ds = 20
+ns0 = 15
+depths = 1
+depthr = 9
+nr = 250
+dr = 1
+nr0 = 0
+nt_interval = 2
+dx = 20.0
+dz = 20.0
+dt = 0.002
+f0 = 10.0
+""")
+    path = str(tmp_path / "input_params.txt")
+    prepare_fwi_parameters(path, cfg)
+    lines = open(path).read().splitlines()
+    assert len(lines) == 38 and lines[0] == "--grid points in x direction (nx)" and lines[1] == "250"
+    assert lines[-2] == "--Dominant frequency (f0)" and lines[-1] == "10.0"
+    p = read_paramfile(path)
+    assert (p.nx, p.nz, p.pml0, p.Lc, p.ns, p.nt, p.nt_interval) == (250, 110, 10, 3, 12, 2001, 2)
+
+
+def test_missing_paramfile(engine_lib, tmp_path):
+    with pytest.raises(FileNotFoundError):
+        read_paramfile(str(tmp_path / "nope.txt"))
+
+
+def _status(engine_lib, p):
+    cp = p.c()
+    return engine_lib.gb_fwi2d_validate(ctypes.byref(cp))
+
+
+def test_validation_codes(engine_lib):
+    good = cases.SMALL["fwi_o8"]["params"]
+    assert _status(engine_lib, good) == _native.OK
+    assert _status(engine_lib, good.replace(laplace_solver=1)) == _native.ENOTSUP
+    assert _status(engine_lib, good.replace(Lc=7)) == _native.EINVAL
+    assert _status(engine_lib, good.replace(nx=0)) == _native.EINVAL
+    assert _status(engine_lib, good.replace(dr=0)) == _native.EINVAL          # 36 receivers in one cell
+    assert _status(engine_lib, good.replace(ns0=10_000)) == _native.EINVAL    # source off the grid
+    assert _status(engine_lib, good.replace(nr=500)) == _native.EINVAL        # receivers off the grid
+    assert _status(engine_lib, good.replace(depths=-100)) == _native.EINVAL
+    assert _status(engine_lib, good.replace(nt_interval=0)) == _native.EINVAL
+    assert _status(engine_lib, good.replace(dt=0.0)) == _native.EINVAL
+
+
+def test_workspace_sizing(engine_lib):
+    p = cases.SMALL["fwi_o8"]["params"]
+    cp = p.c()
+    one = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 2, 1, 0)
+    two = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 2, 2, 0)
+    allr = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 2, 0, 0)
+    fwd = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 2, 0, _native.FLAG_FORWARD_ONLY)
+    assert 0 < one < two <= allr
+    assert fwd < allr
+    # one more resident solve costs three padded fields plus the stored snapshots
+    per = two - one
+    assert per >= 4 * (3 * p.ntp + p.nt_save * p.ncell)
+    bad = p.replace(nx=-1).c()
+    assert engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(bad), 2, 0, 0) == 0
+
+
+def test_batch_rejects_bad_arguments_without_gpu(engine_lib):
+    p = cases.SMALL["fwi_o8"]["params"]
+    cp = p.c()
+    st = engine_lib.gb_fwi2d_batch(ctypes.byref(cp), 0, None, None, None, None, None, 0, 0, None, 0, None)
+    assert st == _native.EINVAL
+    bad = p.replace(laplace_solver=1).c()
+    st = engine_lib.gb_fwi2d_batch(ctypes.byref(bad), 1, 1, 1, None, None, None, 0, 0, 1, 1 << 30, None)
+    assert st == _native.ENOTSUP

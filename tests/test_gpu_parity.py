@@ -1,0 +1,154 @@
+"""GPU engine vs the reference (golden fixtures) and the oracle restatement.
+
+Bars (the tolerances stated for this path):
+  * synthetic data: bit-exact with the reference (relative L2 <= 1e-5 is the
+    stated bar; the engine keeps the reference's FP32 operation order, so the
+    data are compared for equality);
+  * gradient: relative L2 <= 1e-4 against the reference;
+  * misfit: relative error <= 1e-5 against the reference's float32 sum.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.dirname(cases.__file__)
+GRAD_TOL = 1e-4
+DATA_TOL = 1e-5
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, f"{name}.npz"))
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def engine_for(p, **kw):
+    from geopvi_gb300.engine import Fwi2dEngine
+    return Fwi2dEngine(p, device="cuda:0", **kw)
+
+
+def run(eng, vel, obs, **kw):
+    v = torch.from_numpy(np.ascontiguousarray(np.atleast_2d(vel), dtype=np.float32)).cuda()
+    o = torch.from_numpy(np.ascontiguousarray(obs, dtype=np.float32)).cuda()
+    r = eng.run(v, o, **kw)
+    torch.cuda.synchronize()
+    out = {"misfit": r.misfit.cpu().numpy().copy(), "launches": r.launches}
+    if r.grad is not None:
+        out["grad"] = r.grad.cpu().numpy().copy()
+    if r.syn is not None:
+        out["syn"] = r.syn.cpu().numpy().copy()
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(cases.SMALL))
+def test_small_cases_against_reference(engine_lib, cuda, name):
+    z = load(name)
+    p = cases.params_from_npz(z)
+    imaging = int(z["run_fwi"]) == 0
+    eng = engine_for(p, graph=False)
+    fwd = run(eng, z["truth"], np.zeros(p.data_len, np.float32), forward_only=True)
+    assert np.array_equal(fwd["syn"][0], z["obs"]), f"forward data differ: rel {rel(fwd['syn'][0], z['obs']):.3e}"
+    out = run(eng, z["start"], z["obs"], imaging=imaging, want_syn=True)
+    assert np.array_equal(out["syn"][0], z["syn"]), f"syn differs: rel {rel(out['syn'][0], z['syn']):.3e}"
+    e = rel(out["grad"][0], z["grad"])
+    assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
+    m = float(z["misfit"])
+    assert abs(out["misfit"][0] - m) <= DATA_TOL * abs(m)
+
+
+@pytest.mark.parametrize("name", ["fwi_o8", "img_o6", "fwi_ragged"])
+def test_aco2d_dropin(engine_lib, cuda, name, tmp_path):
+    """geopvi_gb300.aco2d.fwi/forward through the C entry points fwi_2D/forward_2D."""
+    from geopvi_gb300 import aco2d
+    from geopvi_gb300.params import write_paramfile
+    z = load(name)
+    p = cases.params_from_npz(z)
+    path = str(tmp_path / "input_param.txt")
+    write_paramfile(path, p)
+    obs = aco2d.forward(z["truth"].astype(np.float64), dim=p.data_len, paramfile=path)
+    assert obs.dtype == np.float32 and np.array_equal(obs, z["obs"])
+    syn, grad = aco2d.fwi(z["start"].astype(np.float64), z["obs"], paramfile=path, is_fwi=int(z["run_fwi"]))
+    assert syn.dtype == np.float32 and grad.dtype == np.float32
+    assert np.array_equal(syn, z["syn"])
+    assert rel(grad, z["grad"]) <= GRAD_TOL
+
+
+def test_batch_of_samples_matches_per_sample_oracle(engine_lib, cuda, oracle):
+    z = load("fwi_o8_nti2")
+    p = cases.params_from_npz(z)
+    op = oracle.Params(**cases.params_to_dict(p))
+    rng = np.random.default_rng(5)
+    vels = np.stack([z["start"], z["truth"], z["start"] * np.float32(1.01),
+                     z["start"] + rng.uniform(-50, 50, p.ncell).astype(np.float32)]).astype(np.float32)
+    eng = engine_for(p, graph=False)
+    out = run(eng, vels, z["obs"], want_syn=True)
+    for i in range(vels.shape[0]):
+        syn_o, grad_o = oracle.fwi_f32(op, vels[i], z["obs"], 1)
+        assert np.array_equal(out["syn"][i], syn_o), f"sample {i}"
+        assert rel(out["grad"][i], grad_o) <= GRAD_TOL, f"sample {i}"
+        syn64, grad64 = oracle.fwi_f64(op, vels[i].astype(np.float64), z["obs"].astype(np.float64), 1)
+        print(f"sample {i}: data err vs FP64 {rel(out['syn'][i], syn64):.2e}, "
+              f"grad err vs FP64 {rel(out['grad'][i], grad64):.2e}, vs reference arithmetic "
+              f"{rel(out['grad'][i], grad_o):.2e}")
+
+
+def test_waves_plain_and_graph_are_identical(engine_lib, cuda):
+    z = load("fwi_o10_nti3")
+    p = cases.params_from_npz(z)
+    vels = np.stack([z["start"], z["truth"], z["start"] * np.float32(0.98)])
+    ref = run(engine_for(p, graph=False), vels, z["obs"], want_syn=True)
+    for kw in (dict(max_resident=1), dict(max_resident=4), dict(plain=True), dict(graph=True)):
+        eng = engine_for(p, **kw)
+        for _ in range(2):  # a graph is captured on the first call and replayed on the second
+            o = run(eng, vels, z["obs"], want_syn=True)
+            assert np.array_equal(o["syn"], ref["syn"]), kw
+            assert np.array_equal(o["grad"], ref["grad"]), kw
+            assert np.array_equal(o["misfit"], ref["misfit"]), kw
+
+
+def test_launch_count(engine_lib, cuda):
+    z = load("fwi_o8")
+    p = cases.params_from_npz(z)
+    o = run(engine_for(p, graph=False), z["start"], z["obs"])
+    # prepare + nt forward + nt adjoint + gradient reduction + 2 misfit kernels
+    assert o["launches"] == 1 + 2 * p.nt + 1 + 2
+
+
+def test_deterministic_repeat(engine_lib, cuda):
+    z = load("fwi_ragged")
+    p = cases.params_from_npz(z)
+    eng = engine_for(p, graph=False)
+    a = run(eng, z["start"], z["obs"], want_syn=True)
+    b = run(eng, z["start"], z["obs"], want_syn=True)
+    assert np.array_equal(a["grad"], b["grad"]) and np.array_equal(a["syn"], b["syn"])
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("name", sorted(cases.FULL))
+def test_full_size_against_reference(engine_lib, cuda, name):
+    z = load(name)
+    p = cases.params_from_npz(z)
+    eng = engine_for(p, graph=False)
+    fwd = run(eng, z["truth"], np.zeros(p.data_len, np.float32), forward_only=True)
+    obs = fwd["syn"][0]
+    sub = lambda d: d.reshape(p.ns, p.nt, p.nr)[0, :, ::cases.SUBSAMPLE_TRACES]
+    assert rel(sub(obs), z["obs_shot0"]) <= DATA_TOL
+    assert hashlib.sha256(obs.tobytes()).hexdigest() == str(z["obs_sha256"]), "forward data not bit-exact"
+    out = run(eng, z["start"], obs, want_syn=True)
+    assert hashlib.sha256(out["syn"][0].tobytes()).hexdigest() == str(z["syn_sha256"])
+    e = rel(out["grad"][0], z["grad"])
+    print(f"{name}: gradient rel L2 vs reference {e:.3e}")
+    assert e <= GRAD_TOL
+    m = float(z["misfit"])
+    assert abs(out["misfit"][0] - m) <= DATA_TOL * abs(m)
