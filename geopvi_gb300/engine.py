@@ -88,17 +88,23 @@ class Fwi2dEngine:
         return int(max(1, min(ninst, fit)))
 
     def _workspace(self, nsamples: int, flags: int) -> tuple[torch.Tensor, int]:
-        resident = self.resident_for(nsamples, flags)
-        key = (nsamples, resident, flags & (_native.FLAG_FORWARD_ONLY | _native.FLAG_CHECKPOINT))
+        """One workspace is held at a time; it is sized once per batch shape
+        (the resident count is not re-derived from free memory while the
+        engine's own workspace occupies part of it)."""
+        key = (nsamples, flags & (_native.FLAG_FORWARD_ONLY | _native.FLAG_CHECKPOINT | _native.FLAG_PLAIN))
         if self._work_key != key:
+            self._work = None
+            self._work_key = None
+            if torch.cuda.is_initialized():
+                torch.cuda.empty_cache()
+            resident = self.resident_for(nsamples, flags)
             nbytes = self.workspace_bytes(nsamples, resident, flags)
             if nbytes == 0:
                 raise _native.EngineError(_native.EINVAL, "gb_fwi2d_workspace_bytes")
-            self._work = None
-            torch.cuda.empty_cache() if torch.cuda.is_initialized() else None
             self._work = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
             self._work_key = key
-        return self._work, resident
+            self._resident = resident
+        return self._work, self._resident
 
     # ---- solve ----
     def run(self, vel: torch.Tensor, obs: torch.Tensor, *, imaging: bool = False,
