@@ -53,12 +53,16 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--hbm-budget-gb", type=float, default=None)
+    ap.add_argument("--nt", type=int, default=None, help="shorten the time axis (profiling runs only)")
     return ap.parse_args()
 
 
-def workload(name: str):
+def workload(name: str, nt: int | None = None):
     from geopvi_gb300 import workloads
-    return {"cfg1": workloads.cfg1, "cfg2": workloads.cfg2, "cfg3": workloads.cfg3}[name]()
+    w = {"cfg1": workloads.cfg1, "cfg2": workloads.cfg2, "cfg3": workloads.cfg3}[name]()
+    if nt:
+        w.params = w.params.replace(nt=nt)
+    return w
 
 
 WORKLOAD_NAMES = {
@@ -173,7 +177,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    w = workload(args.config)
+    w = workload(args.config, args.nt)
     p = w.params
     # observed data from the truth on the host, with the same port (bounded: the sampled shots only)
     from oracle import oracle as O
@@ -238,7 +242,7 @@ def run_gpu(args):
     torch.cuda.set_device(dev)
 
     from geopvi_gb300.engine import Fwi2dEngine
-    w = workload(args.config)
+    w = workload(args.config, args.nt)
     p = w.params
     budget = int(args.hbm_budget_gb * 2**30) if args.hbm_budget_gb else None
     eng = Fwi2dEngine(p, device=dev, graph=False, hbm_budget=budget)
@@ -363,7 +367,8 @@ def run_gpu(args):
             "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded models)",
-            "config": {"workload": WORKLOAD_NAMES[args.config], "samples": nsamples, "shots": p.ns,
+            "config": {"workload": WORKLOAD_NAMES[args.config] + (f" (nt shortened to {p.nt})" if args.nt else ""),
+                       "samples": nsamples, "shots": p.ns,
                        "grid": f"{p.nz}x{p.nx} (padded {p.ntz}x{p.ntx})", "nt": p.nt, "fd_order": 2 * p.Lc,
                        "resident_solves": resident, "waves": -(-ninst // resident),
                        "l2": "inputs larger than L2 (wavefield state of the resident solves >> 129 MB)",

@@ -23,6 +23,7 @@ EINVAL = -22
 ENOTSUP = -95
 ENAN = -1001
 ECUDA = -1002
+ETIMEOUT = -1003
 
 FLAG_IMAGING = 0x1
 FLAG_PLAIN = 0x2
@@ -34,13 +35,14 @@ FLAG_PROFILE = 0x20
 STATUS_NAMES = {ENOENT: "ENOENT (parameter file missing)", ENOMEM: "ENOMEM (device memory)",
                 EINVAL: "EINVAL (invalid parameters or buffers)",
                 ENOTSUP: "ENOTSUP (pseudo-spectral Laplacian not built)",
-                ENAN: "ENAN (NaN in velocity)", ECUDA: "ECUDA (CUDA runtime error)"}
+                ENAN: "ENAN (NaN in velocity)", ECUDA: "ECUDA (CUDA runtime error)",
+                ETIMEOUT: "ETIMEOUT (a bounded device wait gave up)"}
 
 # Every symbol the header declares; tests check that the library exports each.
 EXPORTED_SYMBOLS = (
     "gb_fwi2d_read_params", "gb_fwi2d_validate", "fwi_2D", "forward_2D",
     "gb_fwi2d_workspace_bytes", "gb_fwi2d_batch", "gb_fwi2d_last_launch_count",
-    "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms",
+    "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms", "gb_fwi2d_status",
 )
 
 
@@ -92,6 +94,8 @@ def load() -> ctypes.CDLL:
         L.gb_fwi2d_last_launch_count.restype = ctypes.c_longlong
         L.gb_fwi2d_profile_step_ms.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.gb_fwi2d_profile_step_ms.restype = ctypes.c_double
+        L.gb_fwi2d_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gb_fwi2d_status.restype = ctypes.c_int
         L.gb_fwi2d_release_caches.argtypes = []
         L.gb_fwi2d_release_caches.restype = None
         L.gb_fwi2d_version.argtypes = []

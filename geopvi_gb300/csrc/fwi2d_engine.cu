@@ -7,6 +7,8 @@
 // re-allocates every buffer per sample; here every (sample, shot) solve of a
 // batch advances together, one fused kernel launch per time step, in a
 // caller-owned device workspace, optionally replayed from a CUDA graph.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -110,6 +112,38 @@ static int validate(const gb_fwi2d_params &p)
     return GB_FWI2D_OK;
 }
 
+// Exhaustive proof, per divisor y, that div_const (kernels) returns the
+// correctly rounded x/y: every significand of the binade [1, 2) is checked
+// against the host's IEEE division; the quotient, the FMA remainder and the
+// correction scale exactly with x, so the result holds for every
+// 2^-56 <= |x| <= 2^56 while y stays within [2^-20, 2^20].  Cached per y.
+static bool division_is_exact(float y)
+{
+    static std::mutex m;
+    static std::map<uint32_t, bool> cache;
+    uint32_t key;
+    std::memcpy(&key, &y, sizeof key);
+    {
+        std::lock_guard<std::mutex> lk(m);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    bool ok = std::isfinite(y) && y >= 0x1p-20f && y <= 0x1p20f;
+    const float r = 1.0f / y;
+    for (uint32_t mant = 0; ok && mant < (1u << 23); ++mant) {
+        const uint32_t bits = 0x3F800000u | mant;
+        float x;
+        std::memcpy(&x, &bits, sizeof x);
+        const float q0 = x * r;
+        const float rem = std::fma(-q0, y, x);
+        const float q = std::fma(rem, r, q0);
+        if (q != x / y) ok = false;
+    }
+    std::lock_guard<std::mutex> lk(m);
+    cache[key] = ok;
+    return ok;
+}
+
 static int derive(const gb_fwi2d_params &p, Derived &d)
 {
     int st = validate(p);
@@ -146,6 +180,12 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.dz = p.dz;
     g.dt = p.dt;
     fd_weights(g.Lc, g.fd);
+    g.rdx = 1.0f / p.dx;
+    g.rdz = 1.0f / p.dz;
+    g.rdt = 1.0f / p.dt;
+    g.fast_dx = division_is_exact(p.dx) ? 1 : 0;
+    g.fast_dz = division_is_exact(p.dz) ? 1 : 0;
+    g.fast_dt = division_is_exact(p.dt) ? 1 : 0;
     ricker(p.nt, p.dt, p.f0, d.rik);
     d.w.resize(p.pml0);
     d.omw.resize(p.pml0);
@@ -161,7 +201,7 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
 // ---------------------------------------------------------------------------
 
 struct Layout {
-    size_t vdt, ring, psave, gacc, syn, part, total;
+    size_t status, vdt, ring, psave, gacc, syn, part, total;
     int resident;
 };
 
@@ -177,6 +217,7 @@ static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in
     if (resident <= 0 || resident > ninst) resident = (int)ninst;
     L.resident = resident;
     size_t off = 0;
+    L.status = off; off = align256(off + sizeof(int));
     L.vdt = off;   off = align256(off + sizeof(float) * g.fstride * nsamples);
     L.ring = off;  off = align256(off + sizeof(float) * g.fstride * 3 * resident);
     L.psave = off;
@@ -347,25 +388,69 @@ static int get_tables(const Derived &d, DeviceTables &out)
 // Launch sequence
 // ---------------------------------------------------------------------------
 
-template <int H>
-static void launch_step(bool adj, const Geom &g, const Batch &b, int nres, int k, int it,
-                        float rik_it, cudaStream_t st)
+// cuTensorMapEncodeTiled, fetched from the driver through the runtime.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
-    dim3 grid(g.tiles_x * g.tiles_z, nres), block(kTileX, kBlockZ);
-    if (adj)
-        k_step<H, true><<<grid, block, 0, st>>>(g, b, k, it, rik_it);
-    else
-        k_step<H, false><<<grid, block, 0, st>>>(g, b, k, it, rik_it);
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    return fn;
 }
 
-static void step(bool adj, const Geom &g, const Batch &b, int nres, int k, int it, float rik_it,
+// A 3-D fp32 tensor map over `depth` padded fields [depth][ntz][pitch] with a
+// (box_x, box_z, 1) box; out-of-range elements of a box read as zero.
+static bool make_map(CUtensorMap &m, void *base, const Geom &g, long long depth, int box_x, int box_z)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ntz, (cuuint64_t)depth};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.fstride * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_z, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct Maps {
+    CUtensorMap p1, p0, v;
+};
+
+static bool make_maps(Maps &m, const Geom &g, float *ring, int resident, float *vdt, int nsamples)
+{
+    const int H = g.Lc - 1;
+    return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * H) &&
+           make_map(m.p0, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * kHaloP0) &&
+           make_map(m.v, vdt, g, nsamples, kTileX, kTileZ);
+}
+
+template <int H>
+static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
+                        const StepArgs &sa, cudaStream_t st)
+{
+    const dim3 grid(g.tiles_x * g.tiles_z, nres), block(kThreads);
+    const int smem = TileShape<H>::kSmem;
+    if (adj)
+        k_step<H, true><<<grid, block, smem, st>>>(m.p1, m.p0, m.v, g, b, sa);
+    else
+        k_step<H, false><<<grid, block, smem, st>>>(m.p1, m.p0, m.v, g, b, sa);
+}
+
+static void step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
                  cudaStream_t st)
 {
     switch (g.Lc - 1) {
-    case 3: launch_step<3>(adj, g, b, nres, k, it, rik_it, st); break;
-    case 4: launch_step<4>(adj, g, b, nres, k, it, rik_it, st); break;
-    case 5: launch_step<5>(adj, g, b, nres, k, it, rik_it, st); break;
-    default: launch_step<6>(adj, g, b, nres, k, it, rik_it, st); break;
+    case 3: launch_step<3>(adj, m, g, b, nres, sa, st); break;
+    case 4: launch_step<4>(adj, m, g, b, nres, sa, st); break;
+    case 5: launch_step<5>(adj, m, g, b, nres, sa, st); break;
+    default: launch_step<6>(adj, m, g, b, nres, sa, st); break;
     }
 }
 
@@ -380,6 +465,7 @@ struct Call {
     unsigned flags;
     char *work;
     bool profile;
+    Maps maps;
 };
 
 static int grid_for(long long n, int threads)
@@ -398,6 +484,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
     float *gacc = (float *)(c.work + c.L.gacc);
     float *syn = c.syn ? c.syn : (float *)(c.work + c.L.syn);
     double *part = (double *)(c.work + c.L.part);
+    int *status = (int *)(c.work + c.L.status);
     const bool imaging = (c.flags & GB_FWI2D_IMAGING) != 0;
     const bool plain = (c.flags & GB_FWI2D_PLAIN) != 0;
     const bool fwd_only = (c.flags & GB_FWI2D_FORWARD_ONLY) != 0;
@@ -406,6 +493,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
     k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt,
                                                                                 c.nsamples);
     ++launches;
+    cudaMemsetAsync(status, 0, sizeof(int), st);
     if (!fwd_only) cudaMemsetAsync(gacc, 0, sizeof(float) * g.pstride * ninst, st);
 
     Batch b;
@@ -420,6 +508,8 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.omw = c.tab.omw;
     b.imaging = imaging ? 1 : 0;
     b.store = fwd_only ? 0 : 1;
+    b.status = status;
+    const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
     for (long long i0 = 0; i0 < ninst; i0 += wave) {
@@ -434,8 +524,12 @@ static long long enqueue(const Call &c, cudaStream_t st)
             if (c.profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
                 cudaEventRecord(e0, st);
             for (int k = 0; k < g.nt; ++k) {
-                const int it = adj ? g.nt - 1 - k : k;
-                step(adj, g, b, nres, k, it, adj ? 0.0f : c.d->rik[it], st);
+                StepArgs sa;
+                sa.k = k;
+                sa.it = adj ? g.nt - 1 - k : k;
+                sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
+                sa.rik = adj ? 0.0f : c.d->rik[sa.it];
+                step(adj, maps, g, b, nres, sa, st);
                 ++launches;
             }
             if (e1) {
@@ -605,6 +699,8 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     c.flags = flags;
     c.work = (char *)work;
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
+    if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident, (float *)(c.work + L.vdt), nsamples))
+        return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -620,6 +716,17 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
 }
 
 long long gb_fwi2d_last_launch_count(void) { return t_last_launches; }
+
+int gb_fwi2d_status(const void *work, void *stream)
+{
+    if (!work) return GB_FWI2D_EINVAL;
+    int h = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(&h, work, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GB_FWI2D_ECUDA;
+    return h == kStatusOk ? GB_FWI2D_OK : GB_FWI2D_ETIMEOUT;
+}
 
 double gb_fwi2d_profile_step_ms(long long *launches)
 {
@@ -728,6 +835,8 @@ int host_run(const char *input_file, const float *vel_inner, float *record_syn,
     cudaMemcpyAsync(record_syn, b + o_syn, sizeof(float) * ndata, cudaMemcpyDeviceToHost, s);
     if (with_grad) cudaMemcpyAsync(g.data(), b + o_grad, sizeof(float) * ncell, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return GB_FWI2D_ECUDA;
+    st = gb_fwi2d_status(b + o_work, s);
+    if (st) return st;
     if (with_grad)
         for (size_t i = 0; i < ncell; ++i) grad[i] += g[i];  // the reference accumulates into grad
     return GB_FWI2D_OK;

@@ -8,21 +8,35 @@
 // zero-lag imaging/gradient term (backward_IO, :941-978).  updata_p's copies
 // (:1053-1066) become a rotation of three buffers, so no step copies a field.
 //
+// Data movement: one block owns a 32-column x 64-row tile of one solve.  An
+// elected thread stages the previous two time levels (with halos) and the
+// v*dt tile into shared memory with three TMA tensor loads completing on one
+// mbarrier; each warp then sweeps 16 rows of its 32 columns, keeping the
+// z-stencil window in registers, and writes the new level, the stored
+// snapshot (forward) or the gradient accumulator (adjoint) with coalesced
+// 128-byte row stores.
+//
 // Arithmetic follows the reference operation by operation: __fmul_rn /
-// __fadd_rn / __fsub_rn / __fdiv_rn never contract into FMA, and the
-// boundary blend is carried out in double exactly as the C expression
-// promotes it.  The forward data therefore match the reference bit for bit.
+// __fadd_rn / __fsub_rn never contract into FMA; divisions by the constant
+// dx, dz, dt use a correctly rounded quotient (see div_const); the boundary
+// blend is carried out in double exactly as the C expression promotes it.
+// The forward data therefore match the reference bit for bit.
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace gbfwi {
 
-constexpr int kTileX = 32;   // cells per tile along x: one warp
-constexpr int kTileZ = 32;   // cells per tile along z
-constexpr int kBlockZ = 8;   // threads along z; each owns kTileZ / kBlockZ rows
-constexpr int kMaxHalf = 6;  // stencil half-width Lc-1 for Lc = 4..7
+constexpr int kTileX = 32;    // columns per tile: one warp
+constexpr int kWarpRows = 16; // rows each warp sweeps
+constexpr int kWarps = 4;     // warps per block, stacked in z
+constexpr int kTileZ = kWarpRows * kWarps;  // 64 rows per tile
+constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 16-byte aligned)
+constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
+constexpr int kHaloP0 = 4;    // z halo of the p0 tile (the boundary reads p0 four cells inward)
+constexpr int kThreads = kTileX * kWarps;   // 128
 
 // Geometry shared by every solve of one launch (one parameter set).
 struct Geom {
@@ -34,9 +48,11 @@ struct Geom {
     int ds, s_ix0;       // source column of shot is: s_ix0 + is*ds
     int ns, nt, nti, nt_save;
     int tiles_x, tiles_z;
+    int fast_dx, fast_dz, fast_dt;  // the host proved div_const exact for this divisor
     long long fstride;   // floats per padded field (ntz * pitch)
     long long pstride;   // floats per interior snapshot (nz * ipitch)
     float dx, dz, dt;
+    float rdx, rdz, rdt; // RN(1/dx), RN(1/dz), RN(1/dt)
     float fd[8];
 };
 
@@ -51,15 +67,43 @@ struct Batch {
     float *gacc;         // [nsamples*ns][pstride]
     const float *wtab;   // [pml0]   boundary weights w
     const double *omw;   // [pml0]   1 - w in double
+    int *status;         // device error word (0 = ok)
     int inst0;           // first solve of this wave
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
 };
 
+// Per-launch step data.
+struct StepArgs {
+    int k;        // step within the pass: ring buffers (k%3, (k+1)%3, (k+2)%3) = (p0, p1, p2)
+    int it;       // time index
+    int snap;     // snapshot index it/nt_interval, or -1 when it % nt_interval != 0
+    float rik;    // Ricker value at it (forward)
+};
+
+enum : int { kStatusOk = 0, kStatusTmaTimeout = 1 };
+
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float fq(float a, float b) { return __fdiv_rn(a, b); }
+
+// Correctly rounded x / y for a divisor fixed per launch.  With r = RN(1/y),
+// q0 = RN(x*r) is within an ulp of x/y, the remainder x - q0*y is exact in
+// one FMA, and one correction step q0 + rem*r rounds to RN(x/y) (Markstein's
+// theorem).  The host checks every significand of one binade for the actual
+// y (scale invariance covers 2^-56 <= |x| <= 2^56) before setting `fast`;
+// zeros keep their sign, other magnitudes take the IEEE division.
+__device__ __forceinline__ float div_const(float x, float y, float r, int fast)
+{
+    const float ax = fabsf(x);
+    if (fast && ax >= 0x1p-56f && ax <= 0x1p56f) {
+        const float q0 = __fmul_rn(x, r);
+        const float rem = __fmaf_rn(-q0, y, x);
+        return __fmaf_rn(rem, r, q0);
+    }
+    if (x == 0.0f) return x;
+    return __fdiv_rn(x, y);
+}
 
 // One blend of abc_for_p: a 2nd-order one-way extrapolation from the two
 // previous levels along the inward direction, weighted by w against the
@@ -98,128 +142,235 @@ __device__ __forceinline__ float padded_velocity(const Geom &g, const float *vel
     return vel[(long long)jz * g.nx + jx];
 }
 
-// One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
-// resident slot.  `k` counts steps within the current pass (ring position),
-// `it` is the time index (forward: k, adjoint: nt-1-k).
-template <int H, bool ADJ>
-__global__ void __launch_bounds__(kTileX *kBlockZ)
-    k_step(const Geom g, const Batch b, int k, int it, float rik_it)
+// ---------------------------------------------------------------------------
+// TMA / mbarrier helpers (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
-    constexpr int SW = kTileX + 2 * H;
-    constexpr int SH = kTileZ + 2 * H;
-    __shared__ float s1[SH][SW + 1];
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 3-D tiled TMA load into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
+                                            int z)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Bounded wait: true once phase `parity` completed, false after the limit
+// (the caller records the timeout and skips its work).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 24); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+template <int H>
+struct TileShape {
+    static constexpr int kP1Rows = kTileZ + 2 * H;        // p1 rows staged
+    static constexpr int kP0Rows = kTileZ + 2 * kHaloP0;  // p0 rows staged
+    static constexpr int kP1Floats = kP1Rows * kBoxX;
+    static constexpr int kP0Floats = kP0Rows * kBoxX;
+    static constexpr int kVFloats = kTileZ * kTileX;
+    static constexpr int kBytes = 4 * (kP1Floats + kP0Floats + kVFloats);  // TMA bytes per block
+    static constexpr int kSmem = kBytes + 16;                                // + the mbarrier
+};
+
+// One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
+// resident slot.  Maps: tm_p1 / tm_p0 view the ring as [3*resident][ntz][pitch]
+// with boxes (48, 64+2H) / (48, 72); tm_v views v*dt as [nsamples][ntz][pitch]
+// with box (32, 64).
+template <int H, bool ADJ>
+__global__ void __launch_bounds__(kThreads)
+    k_step(const __grid_constant__ CUtensorMap tm_p1, const __grid_constant__ CUtensorMap tm_p0,
+           const __grid_constant__ CUtensorMap tm_v, const Geom g, const Batch b, const StepArgs sa)
+{
+    using TS = TileShape<H>;
+    // Dynamic shared memory only (no static __shared__), so the tiles start
+    // at the 1024-byte aligned base; each tile is a multiple of 128 bytes.
+    extern __shared__ __align__(1024) float smem[];
+    float *s1 = smem;
+    float *s0 = s1 + TS::kP1Floats;
+    float *sv = s0 + TS::kP0Floats;
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(sv + TS::kVFloats);
 
     const int slot = blockIdx.y;
     const int inst = b.inst0 + slot;
     const int sample = inst / g.ns;
     const int shot = inst - sample * g.ns;
-    const int tile = blockIdx.x;
-    const int tcol = tile % g.tiles_x;
-    const int trow = tile / g.tiles_x;
-    const int col0 = tcol * kTileX;   // memory column
-    const int row0 = trow * kTileZ;   // padded row
+    const int tcol = blockIdx.x % g.tiles_x;
+    const int trow = blockIdx.x / g.tiles_x;
+    const int col0 = tcol * kTileX;
+    const int row0 = trow * kTileZ;
+    const int b0 = sa.k % 3, b1 = (sa.k + 1) % 3, b2 = (sa.k + 2) % 3;
 
-    float *ring = b.ring + (long long)slot * 3 * g.fstride;
-    const float *p0 = ring + (long long)(k % 3) * g.fstride;
-    const float *p1 = ring + (long long)((k + 1) % 3) * g.fstride;
-    float *p2 = ring + (long long)((k + 2) % 3) * g.fstride;
-    const float *vdt = b.vdt + (long long)sample * g.fstride;
-
-    // Stage p1 with a halo of H cells; cells outside the padded grid read 0.
-    const int tid = threadIdx.y * kTileX + threadIdx.x;
-    for (int e = tid; e < SH * SW; e += kTileX * kBlockZ) {
-        const int r = e / SW, c = e - r * SW;
-        const int gz = row0 - H + r;
-        const int gc = col0 - H + c;
-        const int gx = gc - g.xoff;
-        float v = 0.0f;
-        if (gz >= 0 && gz < g.ntz && gx >= 0 && gx < g.ntx) v = p1[(long long)gz * g.pitch + gc];
-        s1[r][c] = v;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, TS::kBytes);
+        tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
+        tma_load_3d(s0, &tm_p0, &bar, col0 - kHaloX, row0 - kHaloP0, slot * 3 + b0);
+        tma_load_3d(sv, &tm_v, &bar, col0, row0, sample);
+    }
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        // The copies may still land in this block's shared memory: wait for
+        // them a second time (bounded) before the block retires.
+        mbar_wait_bounded(&bar, 0);
+        return;
+    }
 
-    const int tx = threadIdx.x;
-    const int col = col0 + tx;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int col = col0 + lane;
     const int ix = col - g.xoff;
     if (ix < 0 || ix >= g.ntx) return;
-    const bool snap = (it % g.nti) == 0;
+
+    // Column-constant facts.
+    const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
+    const bool lef = ix >= g.Lc && ix < g.pml;
+    const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
+    const int wix = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
+    const bool inner_x = ix >= g.pml && ix < g.ntx - g.pml;
     const int s_ix = g.s_ix0 + shot * g.ds;
+    const int cx = lane + kHaloX;
+
+    float *ring = b.ring + (long long)slot * 3 * g.fstride;
+    float *p2 = ring + (long long)b2 * g.fstride;
+
+    const int rr0 = warp * kWarpRows;  // first tile row of this warp
+    // z window of p1 for rows rr0-H .. rr0+H (tile rows; s1 row = tile row + H)
+    float win[2 * H + 1];
+#pragma unroll
+    for (int m = 0; m < 2 * H + 1; ++m) win[m] = s1[(rr0 + m) * kBoxX + cx];
+
+    const long long rec_base = (long long)inst * g.nt * g.nr + (long long)sa.it * g.nr;
+    float *ps = nullptr;
+    float *G = nullptr;
+    if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
+        ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (ix - g.pml);
+        if (ADJ) G = b.gacc + (long long)inst * g.pstride + (ix - g.pml);
+    }
 
 #pragma unroll
-    for (int j = 0; j < kTileZ / kBlockZ; ++j) {
-        const int rr = threadIdx.y + j * kBlockZ;  // row within tile
+    for (int j = 0; j < kWarpRows; ++j) {
+        const int rr = rr0 + j;
         const int iz = row0 + rr;
+        if (j > 0) {
+#pragma unroll
+            for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+            win[2 * H] = s1[(rr + 2 * H) * kBoxX + cx];
+        }
         if (iz >= g.ntz) break;
-        const long long c = (long long)iz * g.pitch + col;
-        const int sr = rr + H, sc = tx + H;
-        const float p1c = s1[sr][sc];
-        const float p0c = p0[c];
-        const float vd = vdt[c];
+        const float p1c = win[H];
+        const int srow1 = (rr + H) * kBoxX;
+        const int srow0 = (rr + kHaloP0) * kBoxX;
+        const float p0c = s0[srow0 + cx];
+        const float vd = sv[rr * kTileX + lane];
         float q = p1c;  // cells the stencil skips keep the previous level
-        if (iz >= g.Lc && iz < g.ntz - g.Lc && ix >= g.Lc && ix < g.ntx - g.Lc) {
+        if (sx && iz >= g.Lc && iz < g.ntz - g.Lc) {
             float lx = fm(g.fd[0], p1c);
             float lz = lx;
 #pragma unroll
             for (int m = 1; m <= H; ++m) {
-                lx = fa(lx, fm(g.fd[m], fa(s1[sr][sc + m], s1[sr][sc - m])));
-                lz = fa(lz, fm(g.fd[m], fa(s1[sr + m][sc], s1[sr - m][sc])));
+                lx = fa(lx, fm(g.fd[m], fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
+                lz = fa(lz, fm(g.fd[m], fa(win[H + m], win[H - m])));
             }
-            const float lap = fa(fq(fq(lx, g.dx), g.dx), fq(fq(lz, g.dz), g.dz));
-            q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), lap));
+            const float ddx = div_const(div_const(lx, g.dx, g.rdx, g.fast_dx), g.dx, g.rdx, g.fast_dx);
+            const float ddz = div_const(div_const(lz, g.dz, g.rdz, g.fast_dz), g.dz, g.rdz, g.fast_dz);
+            q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
         }
         const bool top = iz >= g.Lc && iz < g.pml;
         const bool bot = iz >= g.ntz - g.pml && iz < g.ntz - g.Lc;
-        const bool lef = ix >= g.Lc && ix < g.pml;
-        const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
         if (top || bot || lef || rig) {
-            const float s = fq(vd, g.dx);
+            const float s = div_const(vd, g.dx, g.rdx, g.fast_dx);
             const float t11 = fm(fm(fs(2.0f, s), fs(1.0f, s)), 0.5f);
             const float t12 = fm(s, fs(2.0f, s));
             const float t13 = fm(fm(s, fs(s, 1.0f)), 0.5f);
-            if (top || bot) {
-                const int d = top ? 1 : -1;
-                const long long st = top ? g.pitch : -(long long)g.pitch;
-                const int wi = top ? iz - g.Lc : g.ntz - g.Lc - iz - 1;
-                q = abc_blend(q, t11, t12, t13, p1c, s1[sr + d][sc], s1[sr + 2 * d][sc], p0c,
-                              p0[c + st], p0[c + 2 * st], p0[c + 3 * st], p0[c + 4 * st],
-                              b.wtab[wi], b.omw[wi]);
+            if (top) {
+                const int wi = iz - g.Lc;
+                q = abc_blend(q, t11, t12, t13, p1c, win[H + 1], win[H + 2], p0c,
+                              s0[srow0 + kBoxX + cx], s0[srow0 + 2 * kBoxX + cx],
+                              s0[srow0 + 3 * kBoxX + cx], s0[srow0 + 4 * kBoxX + cx], b.wtab[wi], b.omw[wi]);
+            } else if (bot) {
+                const int wi = g.ntz - g.Lc - iz - 1;
+                q = abc_blend(q, t11, t12, t13, p1c, win[H - 1], win[H - 2], p0c,
+                              s0[srow0 - kBoxX + cx], s0[srow0 - 2 * kBoxX + cx],
+                              s0[srow0 - 3 * kBoxX + cx], s0[srow0 - 4 * kBoxX + cx], b.wtab[wi], b.omw[wi]);
             }
-            if (lef || rig) {
-                const int d = lef ? 1 : -1;
-                const int wi = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
-                q = abc_blend(q, t11, t12, t13, p1c, s1[sr][sc + d], s1[sr][sc + 2 * d], p0c,
-                              p0[c + d], p0[c + 2 * d], p0[c + 3 * d], p0[c + 4 * d], b.wtab[wi],
-                              b.omw[wi]);
+            if (lef) {
+                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + 1], s1[srow1 + cx + 2], p0c,
+                              s0[srow0 + cx + 1], s0[srow0 + cx + 2], s0[srow0 + cx + 3],
+                              s0[srow0 + cx + 4], b.wtab[wix], b.omw[wix]);
+            } else if (rig) {
+                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx - 1], s1[srow1 + cx - 2], p0c,
+                              s0[srow0 + cx - 1], s0[srow0 + cx - 2], s0[srow0 + cx - 3],
+                              s0[srow0 + cx - 4], b.wtab[wix], b.omw[wix]);
             }
         }
-        const long long rec = (long long)inst * g.nt * g.nr + (long long)it * g.nr;
         if (!ADJ) {
             if (iz == g.s_iz && ix == s_ix) {
                 const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
-                q = fa(q, fm(fm(fm(fm(rik_it, g.dt), g.dt), v), v));
+                q = fa(q, fm(fm(fm(fm(sa.rik, g.dt), g.dt), v), v));
             }
         } else if (iz == g.r_iz) {
             const int ir = receiver_of(g, ix);
             if (ir >= 0) {
-                const float o = b.obs[(long long)shot * g.nt * g.nr + (long long)it * g.nr + ir];
-                const float r = b.imaging ? o : fs(b.syn[rec + ir], o);
+                const float o = b.obs[(long long)shot * g.nt * g.nr + (long long)sa.it * g.nr + ir];
+                const float r = b.imaging ? o : fs(b.syn[rec_base + ir], o);
                 const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
                 q = fa(q, fm(fm(fm(fm(r, g.dt), g.dt), v), v));
             }
         }
-        p2[c] = q;
+        p2[(long long)iz * g.pitch + col] = q;
         if (!ADJ && iz == g.r_iz) {
             const int ir = receiver_of(g, ix);
-            if (ir >= 0) b.syn[rec + ir] = q;
+            if (ir >= 0) b.syn[rec_base + ir] = q;
         }
-        const bool inner = iz >= g.pml && iz < g.ntz - g.pml && ix >= g.pml && ix < g.ntx - g.pml;
-        if (snap && inner && (ADJ || b.store)) {
-            const long long pc = (long long)(iz - g.pml) * g.ipitch + (ix - g.pml);
-            float *ps = b.psave + ((long long)slot * g.nt_save + it / g.nti) * g.pstride;
+        if (ps && iz >= g.pml && iz < g.ntz - g.pml) {
+            const long long pc = (long long)(iz - g.pml) * g.ipitch;
             if (!ADJ) {
-                ps[pc] = b.imaging ? q : fq(fq(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt), g.dt);
+                ps[pc] = b.imaging ? q
+                                   : div_const(div_const(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt),
+                                               g.dt, g.rdt, g.fast_dt);
             } else {
-                float *G = b.gacc + (long long)inst * g.pstride;
                 G[pc] = fa(G[pc], fm(ps[pc], q));
             }
         }

@@ -37,6 +37,7 @@ extern "C" {
 #define GB_FWI2D_ENOTSUP (-95)   /* valid in the reference but not built here */
 #define GB_FWI2D_ENAN (-1001)    /* NaN/Inf in the velocity input */
 #define GB_FWI2D_ECUDA (-1002)   /* a CUDA runtime call failed */
+#define GB_FWI2D_ETIMEOUT (-1003) /* a bounded device wait gave up (status word set) */
 
 /* Solver parameters, in the order and with the types read_parameters uses
  * (fdtd2D_modelling.c:1328-1356; file layout written by
@@ -96,6 +97,11 @@ size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_
 int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
                    float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
                    void *work, size_t work_bytes, void *stream);
+
+/* Waits for `stream`, then reads the device status word at the start of a
+ * workspace used by gb_fwi2d_batch: GB_FWI2D_OK, or GB_FWI2D_ETIMEOUT if a
+ * kernel's bounded wait for its staged tiles gave up (results invalid). */
+int gb_fwi2d_status(const void *work, void *stream);
 
 /* Number of kernel launches the last gb_fwi2d_batch call on this thread
  * enqueued (graph replays count the kernels inside the graph). */

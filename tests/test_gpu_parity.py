@@ -152,3 +152,15 @@ def test_full_size_against_reference(engine_lib, cuda, name):
     assert e <= GRAD_TOL
     m = float(z["misfit"])
     assert abs(out["misfit"][0] - m) <= DATA_TOL * abs(m)
+
+
+def test_status_word_clear_after_runs(engine_lib, cuda):
+    """No bounded device wait gave up during a batch (status word at the workspace start)."""
+    import ctypes
+    z = load("fwi_o8")
+    p = cases.params_from_npz(z)
+    eng = engine_for(p, graph=False)
+    run(eng, np.stack([z["start"], z["truth"]]), z["obs"])
+    st = engine_lib.gb_fwi2d_status(ctypes.c_void_p(eng._work.data_ptr()),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
