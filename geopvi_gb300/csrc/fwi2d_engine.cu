@@ -36,8 +36,8 @@ static const double kRefPi = 3.1415926;
 struct Derived {
     Geom g;
     std::vector<float> rik;   // Ricker wavelet per time step
-    std::vector<float> w;     // boundary weights
-    std::vector<double> omw;  // 1 - w, double
+    std::vector<BlendCoef> coef;  // boundary weights w and 1 - w (fdtd2D_modelling.c:227-230)
+    bool blend_fp32 = false;      // every (1 - w) * q is exact in double
 };
 
 static int round_up(int v, int m) { return (v + m - 1) / m * m; }
@@ -144,6 +144,21 @@ static bool division_is_exact(float y)
     return ok;
 }
 
+// Number of significant bits of a finite double (0 for zero).
+static int significant_bits(double v)
+{
+    if (v == 0.0) return 0;
+    int e;
+    double m = std::frexp(std::fabs(v), &e);  // m in [0.5, 1)
+    uint64_t bits = (uint64_t)std::ldexp(m, 53);
+    int n = 53;
+    while (n > 0 && !(bits & 1u)) {
+        bits >>= 1;
+        --n;
+    }
+    return n;
+}
+
 static int derive(const gb_fwi2d_params &p, Derived &d)
 {
     int st = validate(p);
@@ -187,11 +202,17 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.fast_dz = division_is_exact(p.dz) ? 1 : 0;
     g.fast_dt = division_is_exact(p.dt) ? 1 : 0;
     ricker(p.nt, p.dt, p.f0, d.rik);
-    d.w.resize(p.pml0);
-    d.omw.resize(p.pml0);
+    d.coef.resize(p.pml0);
+    d.blend_fp32 = true;
     for (int i = 0; i < p.pml0; ++i) {
-        d.w[i] = (float)(1.0 - 1.0 * i / p.pml0);  // fdtd2D_modelling.c:229
-        d.omw[i] = 1.0 - (double)d.w[i];
+        BlendCoef &c = d.coef[i];
+        c.w = (float)(1.0 - 1.0 * i / p.pml0);  // fdtd2D_modelling.c:229
+        c.omw = 1.0 - (double)c.w;
+        c.bh = (float)c.omw;
+        c.bl = (float)(c.omw - (double)c.bh);
+        // The FP32 blend needs bh + bl == 1 - w exactly and (1 - w) * q exact in
+        // double for any float q: 1 - w may hold at most 53 - 24 = 29 significant bits.
+        if ((double)c.bh + (double)c.bl != c.omw || significant_bits(c.omw) > 29) d.blend_fp32 = false;
     }
     return GB_FWI2D_OK;
 }
@@ -324,8 +345,7 @@ __global__ void k_misfit_final(const double *__restrict__ part, double *__restri
 // ---------------------------------------------------------------------------
 
 struct DeviceTables {
-    float *w = nullptr;
-    double *omw = nullptr;
+    BlendCoef *coef = nullptr;
 };
 
 struct GraphEntry {
@@ -367,16 +387,10 @@ static int get_tables(const Derived &d, DeviceTables &out)
         return GB_FWI2D_OK;
     }
     DeviceTables t;
-    if (cudaMalloc(&t.w, sizeof(float) * d.w.size()) != cudaSuccess) return GB_FWI2D_ENOMEM;
-    if (cudaMalloc(&t.omw, sizeof(double) * d.omw.size()) != cudaSuccess) {
-        cudaFree(t.w);
-        return GB_FWI2D_ENOMEM;
-    }
-    if (cudaMemcpy(t.w, d.w.data(), sizeof(float) * d.w.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(t.omw, d.omw.data(), sizeof(double) * d.omw.size(), cudaMemcpyHostToDevice) !=
-            cudaSuccess) {
-        cudaFree(t.w);
-        cudaFree(t.omw);
+    const size_t bytes = sizeof(BlendCoef) * d.coef.size();
+    if (cudaMalloc(&t.coef, bytes) != cudaSuccess) return GB_FWI2D_ENOMEM;
+    if (cudaMemcpy(t.coef, d.coef.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(t.coef);
         return GB_FWI2D_ECUDA;
     }
     g_tables[key] = t;
@@ -504,8 +518,8 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.ring = ring;
     b.psave = (float *)(c.work + c.L.psave);
     b.gacc = gacc;
-    b.wtab = c.tab.w;
-    b.omw = c.tab.omw;
+    b.coef = c.tab.coef;
+    b.blend_fp32 = c.d->blend_fp32 ? 1 : 0;
     b.imaging = imaging ? 1 : 0;
     b.store = fwd_only ? 0 : 1;
     b.status = status;
@@ -752,8 +766,7 @@ void gb_fwi2d_release_caches(void)
     for (auto &kv : g_graphs) cudaGraphExecDestroy(kv.second.exec);
     g_graphs.clear();
     for (auto &kv : g_tables) {
-        cudaFree(kv.second.w);
-        cudaFree(kv.second.omw);
+        cudaFree(kv.second.coef);
     }
     g_tables.clear();
 }

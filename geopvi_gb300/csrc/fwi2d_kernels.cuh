@@ -27,6 +27,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include "fwi2d_exact.h"
+
 namespace gbfwi {
 
 constexpr int kTileX = 32;    // columns per tile: one warp
@@ -65,8 +67,8 @@ struct Batch {
     float *ring;         // [resident][3][fstride]
     float *psave;        // [resident][nt_save][pstride]
     float *gacc;         // [nsamples*ns][pstride]
-    const float *wtab;   // [pml0]   boundary weights w
-    const double *omw;   // [pml0]   1 - w in double
+    const BlendCoef *coef;  // [pml0] boundary weight w, 1 - w split in floats and as double
+    int blend_fp32;      // the host proved (1 - w) * q exact in double for every weight
     int *status;         // device error word (0 = ok)
     int inst0;           // first solve of this wave
     int imaging;         // run_fwi == 0
@@ -87,31 +89,15 @@ __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); 
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 
-// Correctly rounded x / y for a divisor fixed per launch.  With r = RN(1/y),
-// q0 = RN(x*r) is within an ulp of x/y, the remainder x - q0*y is exact in
-// one FMA, and one correction step q0 + rem*r rounds to RN(x/y) (Markstein's
-// theorem).  The host checks every significand of one binade for the actual
-// y (scale invariance covers 2^-56 <= |x| <= 2^56) before setting `fast`;
-// zeros keep their sign, other magnitudes take the IEEE division.
-__device__ __forceinline__ float div_const(float x, float y, float r, int fast)
-{
-    const float ax = fabsf(x);
-    if (fast && ax >= 0x1p-56f && ax <= 0x1p56f) {
-        const float q0 = __fmul_rn(x, r);
-        const float rem = __fmaf_rn(-q0, y, x);
-        return __fmaf_rn(rem, r, q0);
-    }
-    if (x == 0.0f) return x;
-    return __fdiv_rn(x, y);
-}
-
 // One blend of abc_for_p: a 2nd-order one-way extrapolation from the two
 // previous levels along the inward direction, weighted by w against the
-// current value.  p1a..p1c = p1 at 0,1,2 steps inward; p0a..p0e = p0 at
-// 0..4 steps inward.  The final mix is double, as (1.0-w)*p2 promotes it.
+// current value (fdtd2D_modelling.c:843-849).  p1a..p1c = p1 at 0,1,2 steps
+// inward; p0a..p0e = p0 at 0..4 steps inward.  The extrapolation is float;
+// the final mix is the double expression w*ext + (1.0-w)*q, reproduced
+// exactly by blend_mix.
 __device__ __forceinline__ float abc_blend(float q, float t11, float t12, float t13, float p1a,
                                            float p1b, float p1c, float p0a, float p0b, float p0c,
-                                           float p0d, float p0e, float w, double omw)
+                                           float p0d, float p0e, const BlendCoef &c, int fp32_ok)
 {
     const float a2 = fm(2.0f, t11), b2 = fm(2.0f, t12), e2 = fm(2.0f, t13);
     float ext = fa(fa(fm(a2, p1a), fm(b2, p1b)), fm(e2, p1c));
@@ -120,7 +106,7 @@ __device__ __forceinline__ float abc_blend(float q, float t11, float t12, float 
     ext = fs(ext, fm(fa(fm(t12, t12), fm(a2, t13)), p0c));
     ext = fs(ext, fm(fm(b2, t13), p0d));
     ext = fs(ext, fm(fm(t13, t13), p0e));
-    return __double2float_rn(__dadd_rn((double)fm(w, ext), __dmul_rn(omw, (double)q)));
+    return blend_mix(fm(c.w, ext), q, c, fp32_ok);
 }
 
 // Receiver index of padded column ix on the receiver row, or -1.
@@ -289,15 +275,12 @@ __global__ void __launch_bounds__(kThreads)
         if (ADJ) G = b.gacc + (long long)inst * g.pstride + (ix - g.pml);
     }
 
-#pragma unroll
+    // The row loop is deliberately not unrolled: an unrolled body (with the
+    // boundary blends inlined per row) overflows the instruction cache.
+#pragma unroll 1
     for (int j = 0; j < kWarpRows; ++j) {
         const int rr = rr0 + j;
         const int iz = row0 + rr;
-        if (j > 0) {
-#pragma unroll
-            for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
-            win[2 * H] = s1[(rr + 2 * H) * kBoxX + cx];
-        }
         if (iz >= g.ntz) break;
         const float p1c = win[H];
         const int srow1 = (rr + H) * kBoxX;
@@ -313,8 +296,8 @@ __global__ void __launch_bounds__(kThreads)
                 lx = fa(lx, fm(g.fd[m], fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
                 lz = fa(lz, fm(g.fd[m], fa(win[H + m], win[H - m])));
             }
-            const float ddx = div_const(div_const(lx, g.dx, g.rdx, g.fast_dx), g.dx, g.rdx, g.fast_dx);
-            const float ddz = div_const(div_const(lz, g.dz, g.rdz, g.fast_dz), g.dz, g.rdz, g.fast_dz);
+            const float ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
+            const float ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
             q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
         }
         const bool top = iz >= g.Lc && iz < g.pml;
@@ -328,21 +311,21 @@ __global__ void __launch_bounds__(kThreads)
                 const int wi = iz - g.Lc;
                 q = abc_blend(q, t11, t12, t13, p1c, win[H + 1], win[H + 2], p0c,
                               s0[srow0 + kBoxX + cx], s0[srow0 + 2 * kBoxX + cx],
-                              s0[srow0 + 3 * kBoxX + cx], s0[srow0 + 4 * kBoxX + cx], b.wtab[wi], b.omw[wi]);
+                              s0[srow0 + 3 * kBoxX + cx], s0[srow0 + 4 * kBoxX + cx], b.coef[wi], b.blend_fp32);
             } else if (bot) {
                 const int wi = g.ntz - g.Lc - iz - 1;
                 q = abc_blend(q, t11, t12, t13, p1c, win[H - 1], win[H - 2], p0c,
                               s0[srow0 - kBoxX + cx], s0[srow0 - 2 * kBoxX + cx],
-                              s0[srow0 - 3 * kBoxX + cx], s0[srow0 - 4 * kBoxX + cx], b.wtab[wi], b.omw[wi]);
+                              s0[srow0 - 3 * kBoxX + cx], s0[srow0 - 4 * kBoxX + cx], b.coef[wi], b.blend_fp32);
             }
             if (lef) {
                 q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + 1], s1[srow1 + cx + 2], p0c,
                               s0[srow0 + cx + 1], s0[srow0 + cx + 2], s0[srow0 + cx + 3],
-                              s0[srow0 + cx + 4], b.wtab[wix], b.omw[wix]);
+                              s0[srow0 + cx + 4], b.coef[wix], b.blend_fp32);
             } else if (rig) {
                 q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx - 1], s1[srow1 + cx - 2], p0c,
                               s0[srow0 + cx - 1], s0[srow0 + cx - 2], s0[srow0 + cx - 3],
-                              s0[srow0 + cx - 4], b.wtab[wix], b.omw[wix]);
+                              s0[srow0 + cx - 4], b.coef[wix], b.blend_fp32);
             }
         }
         if (!ADJ) {
@@ -368,11 +351,15 @@ __global__ void __launch_bounds__(kThreads)
             const long long pc = (long long)(iz - g.pml) * g.ipitch;
             if (!ADJ) {
                 ps[pc] = b.imaging ? q
-                                   : div_const(div_const(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt),
-                                               g.dt, g.rdt, g.fast_dt);
+                                   : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
             } else {
                 G[pc] = fa(G[pc], fm(ps[pc], q));
             }
+        }
+        if (j + 1 < kWarpRows) {  // slide the z window one row down
+#pragma unroll
+            for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+            win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
         }
     }
 }

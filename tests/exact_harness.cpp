@@ -1,0 +1,88 @@
+// Host-side harness for the exact FP32 helpers of the GPU kernels
+// (geopvi_gb300/csrc/fwi2d_exact.h).  Built by tests/test_exact_math.py with
+// g++ -ffp-contract=off; every helper is compared with the arithmetic it
+// must reproduce: IEEE float division and the reference's double-precision
+// boundary mix  (float)((double)a + (1.0 - w) * (double)q).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+
+#include "../geopvi_gb300/csrc/fwi2d_exact.h"
+
+using namespace gbfwi;
+
+extern "C" {
+
+// Number of x (all significands of [1,2) times 2^k for k in [klo, khi]) where
+// div_const differs from x / y.
+long long harness_div_mismatches(float y, int klo, int khi)
+{
+    const float r = 1.0f / y;
+    long long bad = 0;
+    for (int k = klo; k <= khi; ++k)
+        for (uint32_t m = 0; m < (1u << 23); m += 7) {
+            const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
+            float x;
+            std::memcpy(&x, &bits, 4);
+            for (float xs : {x, -x}) {
+                if (div_const(xs, y, r, 1) != xs / y) ++bad;
+                if (div_const2(xs, y, r, 1) != (xs / y) / y) ++bad;
+            }
+        }
+    // zeros keep their sign; subnormals and huge values take the slow path
+    for (float xs : {0.0f, -0.0f, 1e-40f, -3e-39f, 1e30f, 3e38f}) {
+        const float a = div_const(xs, y, r, 1), b = xs / y;
+        if (std::memcmp(&a, &b, 4) != 0) ++bad;
+    }
+    return bad;
+}
+
+static float ref_mix(float a, double omw, float q) { return (float)((double)a + omw * (double)q); }
+
+// Random and adversarial trials of blend_mix against the double formula.
+// Returns the number of bitwise mismatches; *fallbacks counts trials that took
+// the double path.
+long long harness_blend_mismatches(int pml0, long long trials, unsigned seed, long long *fallbacks)
+{
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    std::uniform_int_distribution<int> E(-40, 40);
+    long long bad = 0, fb = 0;
+    for (int i = 0; i < pml0; ++i) {
+        BlendCoef c;
+        c.w = (float)(1.0 - 1.0 * i / pml0);
+        c.omw = 1.0 - (double)c.w;
+        c.bh = (float)c.omw;
+        c.bl = (float)(c.omw - (double)c.bh);
+        const bool ok = ((double)c.bh + (double)c.bl) == c.omw;
+        for (long long t = 0; t < trials; ++t) {
+            float q = (float)(U(rng) * std::ldexp(1.0, E(rng)));
+            float ext = (float)(U(rng) * std::ldexp(1.0, E(rng) / 8));
+            if (t % 4 == 1) ext = (float)(-(c.omw * q) / (c.w > 0 ? c.w : 1.0f) * (1.0 + 1e-6 * U(rng)));  // cancellation
+            if (t % 4 == 2) q = std::nextafter(q, 0.0f);
+            if (t % 97 == 3) q = 0.0f;
+            if (t % 89 == 4) q = -0.0f;
+            if (t % 83 == 5) ext = 0.0f;
+            if (t % 79 == 6) q = 1e-41f;  // subnormal
+            const float a = c.w * ext;
+            // near-tie construction: choose q so that a + omw*q sits near a float midpoint
+            if (t % 4 == 3 && c.omw > 0) {
+                const float target = (float)(U(rng) * 4.0);
+                const float next = std::nextafter(target, 10.0f);
+                const double mid = 0.5 * ((double)target + (double)next);
+                q = (float)((mid - (double)a) / c.omw);
+            }
+            const float got = blend_mix(a, q, c, ok ? 1 : 0);
+            const float want = ref_mix(a, c.omw, q);
+            if (std::memcmp(&got, &want, 4) != 0) ++bad;
+            // count the double fallbacks the same way the kernel takes them
+            const float aq = std::fabs(q);
+            if (q != 0.0f && !(aq >= 0x1p-60f && aq <= 0x1p60f)) ++fb;
+        }
+    }
+    if (fallbacks) *fallbacks = fb;
+    return bad;
+}
+
+}  // extern "C"

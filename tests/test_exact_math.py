@@ -1,0 +1,40 @@
+"""Exact FP32 helpers of the kernels, checked on the CPU.
+
+The kernels replace IEEE division by dx, dz, dt with a correction-step
+quotient and the reference's double-precision boundary mix with an FP32
+error-free evaluation (geopvi_gb300/csrc/fwi2d_exact.h).  Both must return
+exactly what the reference's C computes; this compiles the same header for
+the host (no FMA contraction) and compares bit for bit.
+"""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("exact") / "libexact.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
+                    "-o", out, os.path.join(HERE, "exact_harness.cpp")], check=True)
+    L = ctypes.CDLL(out)
+    L.harness_div_mismatches.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
+    L.harness_div_mismatches.restype = ctypes.c_longlong
+    L.harness_blend_mismatches.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
+                                           ctypes.POINTER(ctypes.c_longlong)]
+    L.harness_blend_mismatches.restype = ctypes.c_longlong
+    return L
+
+
+@pytest.mark.parametrize("y", [10.0, 12.0, 9.0, 20.0, 1e-3, 2e-3, 8e-4])
+def test_division_by_grid_constants_is_correctly_rounded(harness, y):
+    assert harness.harness_div_mismatches(y, -40, 40) == 0
+
+
+@pytest.mark.parametrize("pml0", [1, 5, 10, 20, 30])
+def test_blend_matches_double_formula(harness, pml0):
+    fb = ctypes.c_longlong(0)
+    assert harness.harness_blend_mismatches(pml0, 20000, 1234 + pml0, ctypes.byref(fb)) == 0
