@@ -434,15 +434,12 @@ static bool make_map(CUtensorMap &m, void *base, const Geom &g, long long depth,
 }
 
 struct Maps {
-    CUtensorMap p1, p0, v;
+    CUtensorMap p1;
 };
 
-static bool make_maps(Maps &m, const Geom &g, float *ring, int resident, float *vdt, int nsamples)
+static bool make_maps(Maps &m, const Geom &g, float *ring, int resident)
 {
-    const int H = g.Lc - 1;
-    return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * H) &&
-           make_map(m.p0, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * kHaloP0) &&
-           make_map(m.v, vdt, g, nsamples, kTileX, kTileZ);
+    return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * (g.Lc - 1));
 }
 
 template <int H>
@@ -452,9 +449,9 @@ static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, 
     const dim3 grid(g.tiles_x * g.tiles_z, nres), block(kThreads);
     const int smem = TileShape<H>::kSmem;
     if (adj)
-        k_step<H, true><<<grid, block, smem, st>>>(m.p1, m.p0, m.v, g, b, sa);
+        k_step<H, true><<<grid, block, smem, st>>>(m.p1, g, b, sa);
     else
-        k_step<H, false><<<grid, block, smem, st>>>(m.p1, m.p0, m.v, g, b, sa);
+        k_step<H, false><<<grid, block, smem, st>>>(m.p1, g, b, sa);
 }
 
 static void step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
@@ -713,7 +710,7 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     c.flags = flags;
     c.work = (char *)work;
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
-    if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident, (float *)(c.work + L.vdt), nsamples))
+    if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
         return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);
     if (st) return st;

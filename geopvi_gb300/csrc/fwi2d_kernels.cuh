@@ -9,12 +9,12 @@
 // (:1053-1066) become a rotation of three buffers, so no step copies a field.
 //
 // Data movement: one block owns a 32-column x 64-row tile of one solve.  An
-// elected thread stages the previous two time levels (with halos) and the
-// v*dt tile into shared memory with three TMA tensor loads completing on one
-// mbarrier; each warp then sweeps 16 rows of its 32 columns, keeping the
-// z-stencil window in registers, and writes the new level, the stored
-// snapshot (forward) or the gradient accumulator (adjoint) with coalesced
-// 128-byte row stores.
+// elected thread stages the previous time level with its stencil halo into
+// shared memory with one TMA tensor load completing on an mbarrier; each
+// warp then sweeps 16 rows of its 32 columns, keeping the z-stencil window in
+// registers, reading the level before (p0) and v*dt with coalesced loads, and
+// writes the new level, the stored snapshot (forward) or the gradient
+// accumulator (adjoint) with coalesced 128-byte row stores.
 //
 // Arithmetic follows the reference operation by operation: __fmul_rn /
 // __fadd_rn / __fsub_rn never contract into FMA; divisions by the constant
@@ -37,7 +37,6 @@ constexpr int kWarps = 4;     // warps per block, stacked in z
 constexpr int kTileZ = kWarpRows * kWarps;  // 64 rows per tile
 constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 16-byte aligned)
 constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
-constexpr int kHaloP0 = 4;    // z halo of the p0 tile (the boundary reads p0 four cells inward)
 constexpr int kThreads = kTileX * kWarps;   // 128
 
 // Geometry shared by every solve of one launch (one parameter set).
@@ -187,32 +186,42 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 
 template <int H>
 struct TileShape {
-    static constexpr int kP1Rows = kTileZ + 2 * H;        // p1 rows staged
-    static constexpr int kP0Rows = kTileZ + 2 * kHaloP0;  // p0 rows staged
+    static constexpr int kP1Rows = kTileZ + 2 * H;   // p1 rows staged
     static constexpr int kP1Floats = kP1Rows * kBoxX;
-    static constexpr int kP0Floats = kP0Rows * kBoxX;
-    static constexpr int kVFloats = kTileZ * kTileX;
-    static constexpr int kBytes = 4 * (kP1Floats + kP0Floats + kVFloats);  // TMA bytes per block
-    static constexpr int kSmem = kBytes + 16;                                // + the mbarrier
+    static constexpr int kBytes = 4 * kP1Floats;     // TMA bytes per block
+    static constexpr int kSmem = kBytes + 16;        // + the mbarrier
 };
 
+// Exact two-step quotients (x/d)/d for both Laplacian terms; one range test
+// covers the four divisions of a cell, the rare rest takes div_const2.
+__device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Geom &g, float &ddx, float &ddz)
+{
+    const float ax = fabsf(lx), az = fabsf(lz);
+    if (g.fast_dx & g.fast_dz & (fminf(ax, az) >= kDiv2Lo) & (fmaxf(ax, az) <= kDiv2Hi)) {
+        ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
+        ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
+    } else {
+        ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
+    }
+}
+
 // One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
-// resident slot.  Maps: tm_p1 / tm_p0 view the ring as [3*resident][ntz][pitch]
-// with boxes (48, 64+2H) / (48, 72); tm_v views v*dt as [nsamples][ntz][pitch]
-// with box (32, 64).
+// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with a
+// (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
+// and v*dt are read once per cell with coalesced read-only loads (the
+// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
+// per block and lets 16 blocks share an SM.
 template <int H, bool ADJ>
 __global__ void __launch_bounds__(kThreads)
-    k_step(const __grid_constant__ CUtensorMap tm_p1, const __grid_constant__ CUtensorMap tm_p0,
-           const __grid_constant__ CUtensorMap tm_v, const Geom g, const Batch b, const StepArgs sa)
+    k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
-    // Dynamic shared memory only (no static __shared__), so the tiles start
-    // at the 1024-byte aligned base; each tile is a multiple of 128 bytes.
+    // Dynamic shared memory only (no static __shared__), so the tile starts
+    // at the 1024-byte aligned base.
     extern __shared__ __align__(1024) float smem[];
     float *s1 = smem;
-    float *s0 = s1 + TS::kP1Floats;
-    float *sv = s0 + TS::kP0Floats;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(sv + TS::kVFloats);
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
 
     const int slot = blockIdx.y;
     const int inst = b.inst0 + slot;
@@ -232,22 +241,36 @@ __global__ void __launch_bounds__(kThreads)
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&bar, TS::kBytes);
         tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
-        tma_load_3d(s0, &tm_p0, &bar, col0 - kHaloX, row0 - kHaloP0, slot * 3 + b0);
-        tma_load_3d(sv, &tm_v, &bar, col0, row0, sample);
-    }
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
-        // The copies may still land in this block's shared memory: wait for
-        // them a second time (bounded) before the block retires.
-        mbar_wait_bounded(&bar, 0);
-        return;
     }
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int col = col0 + lane;
     const int ix = col - g.xoff;
-    if (ix < 0 || ix >= g.ntx) return;
+    const bool live = ix >= 0 && ix < g.ntx;
+    float *ring = b.ring + (long long)slot * 3 * g.fstride;
+    const float *__restrict__ p0 = ring + (long long)b0 * g.fstride;
+    float *p2 = ring + (long long)b2 * g.fstride;
+    const float *__restrict__ vdt = b.vdt + (long long)sample * g.fstride;
+    const int rr0 = warp * kWarpRows;  // first tile row of this warp
+    const int iz0 = row0 + rr0;
+
+    // Issue this thread's first p0 / v*dt loads while the tile is in flight.
+    const long long c0 = (long long)iz0 * g.pitch + col;
+    float p0_next = 0.0f, vd_next = 0.0f;
+    if (live && iz0 < g.ntz) {
+        p0_next = __ldg(p0 + c0);
+        vd_next = __ldg(vdt + c0);
+    }
+
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        // The copy may still land in this block's shared memory: wait for it
+        // a second time (bounded) before the block retires.
+        mbar_wait_bounded(&bar, 0);
+        return;
+    }
+    if (!live) return;
 
     // Column-constant facts.
     const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
@@ -255,19 +278,17 @@ __global__ void __launch_bounds__(kThreads)
     const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
     const int wix = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
     const bool inner_x = ix >= g.pml && ix < g.ntx - g.pml;
-    const int s_ix = g.s_ix0 + shot * g.ds;
+    const bool src_col = ix == g.s_ix0 + shot * g.ds;
     const int cx = lane + kHaloX;
+    float fd[H + 1];
+#pragma unroll
+    for (int m = 0; m <= H; ++m) fd[m] = g.fd[m];
 
-    float *ring = b.ring + (long long)slot * 3 * g.fstride;
-    float *p2 = ring + (long long)b2 * g.fstride;
-
-    const int rr0 = warp * kWarpRows;  // first tile row of this warp
     // z window of p1 for rows rr0-H .. rr0+H (tile rows; s1 row = tile row + H)
     float win[2 * H + 1];
 #pragma unroll
     for (int m = 0; m < 2 * H + 1; ++m) win[m] = s1[(rr0 + m) * kBoxX + cx];
 
-    const long long rec_base = (long long)inst * g.nt * g.nr + (long long)sa.it * g.nr;
     float *ps = nullptr;
     float *G = nullptr;
     if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
@@ -280,24 +301,28 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll 1
     for (int j = 0; j < kWarpRows; ++j) {
         const int rr = rr0 + j;
-        const int iz = row0 + rr;
+        const int iz = iz0 + j;
         if (iz >= g.ntz) break;
+        const long long c = (long long)iz * g.pitch + col;
+        const float p0c = p0_next;
+        const float vd = vd_next;
+        if (j + 1 < kWarpRows && iz + 1 < g.ntz) {  // prefetch the next row
+            p0_next = __ldg(p0 + c + g.pitch);
+            vd_next = __ldg(vdt + c + g.pitch);
+        }
         const float p1c = win[H];
         const int srow1 = (rr + H) * kBoxX;
-        const int srow0 = (rr + kHaloP0) * kBoxX;
-        const float p0c = s0[srow0 + cx];
-        const float vd = sv[rr * kTileX + lane];
         float q = p1c;  // cells the stencil skips keep the previous level
         if (sx && iz >= g.Lc && iz < g.ntz - g.Lc) {
-            float lx = fm(g.fd[0], p1c);
+            float lx = fm(fd[0], p1c);
             float lz = lx;
 #pragma unroll
             for (int m = 1; m <= H; ++m) {
-                lx = fa(lx, fm(g.fd[m], fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
-                lz = fa(lz, fm(g.fd[m], fa(win[H + m], win[H - m])));
+                lx = fa(lx, fm(fd[m], fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
+                lz = fa(lz, fm(fd[m], fa(win[H + m], win[H - m])));
             }
-            const float ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
-            const float ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
+            float ddx, ddz;
+            laplacian_quotients(lx, lz, g, ddx, ddz);
             q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
         }
         const bool top = iz >= g.Lc && iz < g.pml;
@@ -307,51 +332,46 @@ __global__ void __launch_bounds__(kThreads)
             const float t11 = fm(fm(fs(2.0f, s), fs(1.0f, s)), 0.5f);
             const float t12 = fm(s, fs(2.0f, s));
             const float t13 = fm(fm(s, fs(s, 1.0f)), 0.5f);
-            if (top) {
-                const int wi = iz - g.Lc;
-                q = abc_blend(q, t11, t12, t13, p1c, win[H + 1], win[H + 2], p0c,
-                              s0[srow0 + kBoxX + cx], s0[srow0 + 2 * kBoxX + cx],
-                              s0[srow0 + 3 * kBoxX + cx], s0[srow0 + 4 * kBoxX + cx], b.coef[wi], b.blend_fp32);
-            } else if (bot) {
-                const int wi = g.ntz - g.Lc - iz - 1;
-                q = abc_blend(q, t11, t12, t13, p1c, win[H - 1], win[H - 2], p0c,
-                              s0[srow0 - kBoxX + cx], s0[srow0 - 2 * kBoxX + cx],
-                              s0[srow0 - 3 * kBoxX + cx], s0[srow0 - 4 * kBoxX + cx], b.coef[wi], b.blend_fp32);
+            if (top || bot) {
+                const int d = top ? 1 : -1;
+                const long long st = top ? g.pitch : -(long long)g.pitch;
+                const int wi = top ? iz - g.Lc : g.ntz - g.Lc - iz - 1;
+                q = abc_blend(q, t11, t12, t13, p1c, top ? win[H + 1] : win[H - 1],
+                              top ? win[H + 2] : win[H - 2], p0c, __ldg(p0 + c + st), __ldg(p0 + c + 2 * st),
+                              __ldg(p0 + c + 3 * st), __ldg(p0 + c + 4 * st), b.coef[wi], b.blend_fp32);
+                (void)d;
             }
-            if (lef) {
-                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + 1], s1[srow1 + cx + 2], p0c,
-                              s0[srow0 + cx + 1], s0[srow0 + cx + 2], s0[srow0 + cx + 3],
-                              s0[srow0 + cx + 4], b.coef[wix], b.blend_fp32);
-            } else if (rig) {
-                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx - 1], s1[srow1 + cx - 2], p0c,
-                              s0[srow0 + cx - 1], s0[srow0 + cx - 2], s0[srow0 + cx - 3],
-                              s0[srow0 + cx - 4], b.coef[wix], b.blend_fp32);
+            if (lef || rig) {
+                const int d = lef ? 1 : -1;
+                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + d], s1[srow1 + cx + 2 * d], p0c,
+                              __ldg(p0 + c + d), __ldg(p0 + c + 2 * d), __ldg(p0 + c + 3 * d),
+                              __ldg(p0 + c + 4 * d), b.coef[wix], b.blend_fp32);
             }
         }
         if (!ADJ) {
-            if (iz == g.s_iz && ix == s_ix) {
+            if (iz == g.s_iz && src_col) {
                 const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
                 q = fa(q, fm(fm(fm(fm(sa.rik, g.dt), g.dt), v), v));
             }
         } else if (iz == g.r_iz) {
             const int ir = receiver_of(g, ix);
             if (ir >= 0) {
-                const float o = b.obs[(long long)shot * g.nt * g.nr + (long long)sa.it * g.nr + ir];
-                const float r = b.imaging ? o : fs(b.syn[rec_base + ir], o);
+                const long long rec = ((long long)inst * g.nt + sa.it) * g.nr + ir;
+                const float o = b.obs[((long long)shot * g.nt + sa.it) * g.nr + ir];
+                const float r = b.imaging ? o : fs(b.syn[rec], o);
                 const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
                 q = fa(q, fm(fm(fm(fm(r, g.dt), g.dt), v), v));
             }
         }
-        p2[(long long)iz * g.pitch + col] = q;
+        p2[c] = q;
         if (!ADJ && iz == g.r_iz) {
             const int ir = receiver_of(g, ix);
-            if (ir >= 0) b.syn[rec_base + ir] = q;
+            if (ir >= 0) b.syn[((long long)inst * g.nt + sa.it) * g.nr + ir] = q;
         }
         if (ps && iz >= g.pml && iz < g.ntz - g.pml) {
             const long long pc = (long long)(iz - g.pml) * g.ipitch;
             if (!ADJ) {
-                ps[pc] = b.imaging ? q
-                                   : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+                ps[pc] = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
             } else {
                 G[pc] = fa(G[pc], fm(ps[pc], q));
             }
