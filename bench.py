@@ -278,6 +278,7 @@ def run_gpu(args):
     barrier()
     ms = e0.elapsed_time(e1)
     step_ms, step_launches = eng.step_profile()
+    device_status = eng.status()
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -377,7 +378,7 @@ def run_gpu(args):
             "plain": plain,
             "batched_vs_plain": (sgrad / world) / plain["sample_gradients_per_s"] if plain else None,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": launches,
+            "gpu_launches": launches, "device_status": device_status,
         }
         print(json.dumps(out), flush=True)
     if world > 1:

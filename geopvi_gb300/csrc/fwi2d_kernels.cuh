@@ -206,104 +206,102 @@ __device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Ge
     }
 }
 
-// One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
-// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with a
-// (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
-// and v*dt are read once per cell with coalesced read-only loads (the
-// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
-// per block and lets 16 blocks share an SM.
+// Per-warp view of one step: where the warp's 16 x 32 cells live and which
+// buffers they read and write.
+struct WarpCtx {
+    const float *s1;             // staged p1 tile (48 columns x (64 + 2H) rows)
+    const float *p0;             // previous-previous level, padded field
+    float *p2;                   // new level, padded field
+    const float *vdt;            // v*dt, padded field
+    float *ps;                   // this column's stored snapshot (interior), or null
+    float *G;                    // this column's gradient accumulator (adjoint), or null
+    long long c;                 // field offset of the warp's first cell of this lane
+    int rr0, iz0, ix, cx, lane;  // first tile row, first padded row, column, staged column, lane
+    int inst, sample, shot;
+};
+
+// Interior sweep: every cell of the warp is inside the interior of the
+// padded grid, away from the absorbing strips, the source and the receivers,
+// so each row is the stencil, the exact quotients, the new level and the
+// snapshot / gradient term, without per-cell region tests.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads)
-    k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
+__device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
+                                               const float (&fd)[H + 1], float p0_next, float vd_next)
 {
-    using TS = TileShape<H>;
-    // Dynamic shared memory only (no static __shared__), so the tile starts
-    // at the 1024-byte aligned base.
-    extern __shared__ __align__(1024) float smem[];
-    float *s1 = smem;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
-
-    const int slot = blockIdx.y;
-    const int inst = b.inst0 + slot;
-    const int sample = inst / g.ns;
-    const int shot = inst - sample * g.ns;
-    const int tcol = blockIdx.x % g.tiles_x;
-    const int trow = blockIdx.x / g.tiles_x;
-    const int col0 = tcol * kTileX;
-    const int row0 = trow * kTileZ;
-    const int b0 = sa.k % 3, b1 = (sa.k + 1) % 3, b2 = (sa.k + 2) % 3;
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
+    float win[2 * H + 1];
+#pragma unroll
+    for (int m = 0; m < 2 * H + 1; ++m) win[m] = w.s1[(w.rr0 + m) * kBoxX + w.cx];
+    const float *p0 = w.p0 + w.c;
+    const float *vdt = w.vdt + w.c;
+    float *p2 = w.p2 + w.c;
+    float *ps = w.ps ? w.ps + (long long)(w.iz0 - g.pml) * g.ipitch : nullptr;
+    float *G = w.G ? w.G + (long long)(w.iz0 - g.pml) * g.ipitch : nullptr;
+    const float *srow = w.s1 + (w.rr0 + H) * kBoxX + w.cx;
+#pragma unroll 1
+    for (int j = 0; j < kWarpRows; ++j) {
+        const float p0c = p0_next, vd = vd_next;
+        p0 += g.pitch;
+        vdt += g.pitch;
+        if (j + 1 < kWarpRows) {  // rows stay inside the grid: the warp is interior
+            p0_next = __ldg(p0);
+            vd_next = __ldg(vdt);
+        }
+        const float p1c = win[H];
+        float lx = fm(fd[0], p1c);
+        float lz = lx;
+#pragma unroll
+        for (int m = 1; m <= H; ++m) {
+            lx = fa(lx, fm(fd[m], fa(srow[m], srow[-m])));
+            lz = fa(lz, fm(fd[m], fa(win[H + m], win[H - m])));
+        }
+        float ddx, ddz;
+        laplacian_quotients(lx, lz, g, ddx, ddz);
+        const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
+        *p2 = q;
+        p2 += g.pitch;
+        if (ps) {
+            if (!ADJ)
+                *ps = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+            else
+                *G = fa(*G, fm(*ps, q));
+            ps += g.ipitch;
+            if (ADJ) G += g.ipitch;
+        }
+#pragma unroll
+        for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+        srow += kBoxX;
+        if (j + 1 < kWarpRows) win[2 * H] = srow[H * kBoxX];
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, TS::kBytes);
-        tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
-    }
+}
 
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int col = col0 + lane;
-    const int ix = col - g.xoff;
-    const bool live = ix >= 0 && ix < g.ntx;
-    float *ring = b.ring + (long long)slot * 3 * g.fstride;
-    const float *__restrict__ p0 = ring + (long long)b0 * g.fstride;
-    float *p2 = ring + (long long)b2 * g.fstride;
-    const float *__restrict__ vdt = b.vdt + (long long)sample * g.fstride;
-    const int rr0 = warp * kWarpRows;  // first tile row of this warp
-    const int iz0 = row0 + rr0;
-
-    // Issue this thread's first p0 / v*dt loads while the tile is in flight.
-    const long long c0 = (long long)iz0 * g.pitch + col;
-    float p0_next = 0.0f, vd_next = 0.0f;
-    if (live && iz0 < g.ntz) {
-        p0_next = __ldg(p0 + c0);
-        vd_next = __ldg(vdt + c0);
-    }
-
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
-        // The copy may still land in this block's shared memory: wait for it
-        // a second time (bounded) before the block retires.
-        mbar_wait_bounded(&bar, 0);
-        return;
-    }
-    if (!live) return;
-
-    // Column-constant facts.
+// General sweep for warps that touch the rim, an absorbing strip, the
+// source row or the receiver row: the same arithmetic with every region
+// test of the reference's loops.
+template <int H, bool ADJ>
+__device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
+                                           const float (&fd)[H + 1], float p0_next, float vd_next)
+{
+    const int ix = w.ix;
     const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
     const bool lef = ix >= g.Lc && ix < g.pml;
     const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
     const int wix = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
-    const bool inner_x = ix >= g.pml && ix < g.ntx - g.pml;
-    const bool src_col = ix == g.s_ix0 + shot * g.ds;
-    const int cx = lane + kHaloX;
-    float fd[H + 1];
-#pragma unroll
-    for (int m = 0; m <= H; ++m) fd[m] = g.fd[m];
+    const bool src_col = ix == g.s_ix0 + w.shot * g.ds;
+    const int cx = w.cx;
+    const float *s1 = w.s1;
+    const float *p0 = w.p0;
+    const float *vdt = w.vdt;
 
-    // z window of p1 for rows rr0-H .. rr0+H (tile rows; s1 row = tile row + H)
     float win[2 * H + 1];
 #pragma unroll
-    for (int m = 0; m < 2 * H + 1; ++m) win[m] = s1[(rr0 + m) * kBoxX + cx];
+    for (int m = 0; m < 2 * H + 1; ++m) win[m] = s1[(w.rr0 + m) * kBoxX + cx];
 
-    float *ps = nullptr;
-    float *G = nullptr;
-    if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
-        ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (ix - g.pml);
-        if (ADJ) G = b.gacc + (long long)inst * g.pstride + (ix - g.pml);
-    }
-
-    // The row loop is deliberately not unrolled: an unrolled body (with the
-    // boundary blends inlined per row) overflows the instruction cache.
 #pragma unroll 1
     for (int j = 0; j < kWarpRows; ++j) {
-        const int rr = rr0 + j;
-        const int iz = iz0 + j;
+        const int rr = w.rr0 + j;
+        const int iz = w.iz0 + j;
         if (iz >= g.ntz) break;
-        const long long c = (long long)iz * g.pitch + col;
+        const long long c = w.c + (long long)j * g.pitch;
         const float p0c = p0_next;
         const float vd = vd_next;
         if (j + 1 < kWarpRows && iz + 1 < g.ntz) {  // prefetch the next row
@@ -332,16 +330,14 @@ __global__ void __launch_bounds__(kThreads)
             const float t11 = fm(fm(fs(2.0f, s), fs(1.0f, s)), 0.5f);
             const float t12 = fm(s, fs(2.0f, s));
             const float t13 = fm(fm(s, fs(s, 1.0f)), 0.5f);
-            if (top || bot) {
-                const int d = top ? 1 : -1;
+            if (top || bot) {  // abc_for_p top / bottom passes (fdtd2D_modelling.c:837-867)
                 const long long st = top ? g.pitch : -(long long)g.pitch;
                 const int wi = top ? iz - g.Lc : g.ntz - g.Lc - iz - 1;
-                q = abc_blend(q, t11, t12, t13, p1c, top ? win[H + 1] : win[H - 1],
-                              top ? win[H + 2] : win[H - 2], p0c, __ldg(p0 + c + st), __ldg(p0 + c + 2 * st),
-                              __ldg(p0 + c + 3 * st), __ldg(p0 + c + 4 * st), b.coef[wi], b.blend_fp32);
-                (void)d;
+                q = abc_blend(q, t11, t12, t13, p1c, top ? win[H + 1] : win[H - 1], top ? win[H + 2] : win[H - 2],
+                              p0c, __ldg(p0 + c + st), __ldg(p0 + c + 2 * st), __ldg(p0 + c + 3 * st),
+                              __ldg(p0 + c + 4 * st), b.coef[wi], b.blend_fp32);
             }
-            if (lef || rig) {
+            if (lef || rig) {  // left / right passes (:869-899), after top / bottom
                 const int d = lef ? 1 : -1;
                 q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + d], s1[srow1 + cx + 2 * d], p0c,
                               __ldg(p0 + c + d), __ldg(p0 + c + 2 * d), __ldg(p0 + c + 3 * d),
@@ -349,32 +345,31 @@ __global__ void __launch_bounds__(kThreads)
             }
         }
         if (!ADJ) {
-            if (iz == g.s_iz && src_col) {
-                const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
+            if (iz == g.s_iz && src_col) {  // forward_IO source injection (:910)
+                const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
                 q = fa(q, fm(fm(fm(fm(sa.rik, g.dt), g.dt), v), v));
             }
-        } else if (iz == g.r_iz) {
+        } else if (iz == g.r_iz) {  // backward_IO residual injection (:949-959)
             const int ir = receiver_of(g, ix);
             if (ir >= 0) {
-                const long long rec = ((long long)inst * g.nt + sa.it) * g.nr + ir;
-                const float o = b.obs[((long long)shot * g.nt + sa.it) * g.nr + ir];
+                const long long rec = ((long long)w.inst * g.nt + sa.it) * g.nr + ir;
+                const float o = b.obs[((long long)w.shot * g.nt + sa.it) * g.nr + ir];
                 const float r = b.imaging ? o : fs(b.syn[rec], o);
-                const float v = padded_velocity(g, b.vel + (long long)sample * g.nx * g.nz, iz, ix);
+                const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
                 q = fa(q, fm(fm(fm(fm(r, g.dt), g.dt), v), v));
             }
         }
-        p2[c] = q;
-        if (!ADJ && iz == g.r_iz) {
+        w.p2[c] = q;
+        if (!ADJ && iz == g.r_iz) {  // forward_IO receiver sampling (:930-938)
             const int ir = receiver_of(g, ix);
-            if (ir >= 0) b.syn[((long long)inst * g.nt + sa.it) * g.nr + ir] = q;
+            if (ir >= 0) b.syn[((long long)w.inst * g.nt + sa.it) * g.nr + ir] = q;
         }
-        if (ps && iz >= g.pml && iz < g.ntz - g.pml) {
+        if (w.ps && iz >= g.pml && iz < g.ntz - g.pml) {
             const long long pc = (long long)(iz - g.pml) * g.ipitch;
-            if (!ADJ) {
-                ps[pc] = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
-            } else {
-                G[pc] = fa(G[pc], fm(ps[pc], q));
-            }
+            if (!ADJ)
+                w.ps[pc] = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+            else
+                w.G[pc] = fa(w.G[pc], fm(w.ps[pc], q));
         }
         if (j + 1 < kWarpRows) {  // slide the z window one row down
 #pragma unroll
@@ -382,6 +377,98 @@ __global__ void __launch_bounds__(kThreads)
             win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
         }
     }
+}
+
+// One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
+// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with a
+// (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
+// and v*dt are read once per cell with coalesced read-only loads (the
+// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
+// per block.  Each warp then sweeps its 16 rows with the interior or the
+// general row body, a warp-uniform choice.
+template <int H, bool ADJ>
+__global__ void __launch_bounds__(kThreads, 8)
+    k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
+{
+    using TS = TileShape<H>;
+    // Dynamic shared memory only (no static __shared__), so the tile starts
+    // at the 1024-byte aligned base.
+    extern __shared__ __align__(1024) float smem[];
+    float *s1 = smem;
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
+
+    const int slot = blockIdx.y;
+    const int tcol = blockIdx.x % g.tiles_x;
+    const int trow = blockIdx.x / g.tiles_x;
+    const int col0 = tcol * kTileX;
+    const int row0 = trow * kTileZ;
+    const int b0 = sa.k % 3, b1 = (sa.k + 1) % 3, b2 = (sa.k + 2) % 3;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, TS::kBytes);
+        tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
+    }
+
+    WarpCtx w;
+    w.inst = b.inst0 + slot;
+    w.sample = w.inst / g.ns;
+    w.shot = w.inst - w.sample * g.ns;
+    w.lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int col = col0 + w.lane;
+    w.ix = col - g.xoff;
+    w.cx = w.lane + kHaloX;
+    w.rr0 = warp * kWarpRows;
+    w.iz0 = row0 + w.rr0;
+    w.s1 = s1;
+    const bool live = w.ix >= 0 && w.ix < g.ntx;
+    float *ring = b.ring + (long long)slot * 3 * g.fstride;
+    w.p0 = ring + (long long)b0 * g.fstride;
+    w.p2 = ring + (long long)b2 * g.fstride;
+    w.vdt = b.vdt + (long long)w.sample * g.fstride;
+    w.c = (long long)w.iz0 * g.pitch + col;
+
+    // Issue this thread's first p0 / v*dt loads while the tile is in flight.
+    float p0_next = 0.0f, vd_next = 0.0f;
+    if (live && w.iz0 < g.ntz) {
+        p0_next = __ldg(w.p0 + w.c);
+        vd_next = __ldg(w.vdt + w.c);
+    }
+
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        // The copy may still land in this block's shared memory: wait for it
+        // a second time (bounded) before the block retires.
+        mbar_wait_bounded(&bar, 0);
+        return;
+    }
+    if (!live || w.iz0 >= g.ntz) return;
+
+    const bool inner_x = w.ix >= g.pml && w.ix < g.ntx - g.pml;
+    w.ps = nullptr;
+    w.G = nullptr;
+    if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
+        w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml);
+        if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml);
+    }
+    float fd[H + 1];
+#pragma unroll
+    for (int m = 0; m <= H; ++m) fd[m] = g.fd[m];
+
+    // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
+    const int ix0 = col0 - g.xoff;
+    const bool interior = w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml && ix0 >= g.pml &&
+                          ix0 + kTileX <= g.ntx - g.pml && (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
+                          (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
+    if (interior)
+        sweep_interior<H, ADJ>(g, b, sa, w, fd, p0_next, vd_next);
+    else
+        sweep_general<H, ADJ>(g, b, sa, w, fd, p0_next, vd_next);
 }
 
 }  // namespace gbfwi

@@ -161,6 +161,14 @@ class Fwi2dEngine:
         return RunResult(misfit=misfit, grad=grad, syn=syn,
                          launches=int(self.lib.gb_fwi2d_last_launch_count()))
 
+    def status(self) -> int:
+        """Device status word of the current workspace after the queued work
+        finishes: 0, or the C ABI's ETIMEOUT if a bounded wait gave up."""
+        if self._work is None:
+            return _native.OK
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        return int(self.lib.gb_fwi2d_status(ctypes.c_void_p(self._work.data_ptr()), ctypes.c_void_p(stream)))
+
     def step_profile(self) -> tuple[float, int]:
         """(device ms, launches) of the time-step kernels of every
         ``run(..., profile=True)`` on this thread since the previous read."""
