@@ -42,35 +42,23 @@ struct Derived {
 
 static int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
-// fd_coefficient (fdtd2D_modelling.c:1272-1326): double literals stored as float.
+// fd_coefficient (fdtd2D_modelling.c:1272-1326): double literals stored as
+// float, from the same table the kernels use as immediates.
+template <int H>
+static void copy_weights(float *fd)
+{
+    for (int i = 0; i <= H; ++i) fd[i] = fd_weight<H>(i);
+}
+
 static void fd_weights(int Lc, float *fd)
 {
     for (int i = 0; i < 8; ++i) fd[i] = 0.0f;
     switch (Lc) {
-    case 4:
-        fd[3] = (float)(1.0 / 90); fd[2] = (float)(-3.0 / 20); fd[1] = 1.5f;
-        fd[0] = (float)(-49.0 / 18);
-        break;
-    case 5:
-        fd[4] = (float)(-1.0 / 560); fd[3] = (float)(8.0 / 315); fd[2] = (float)(-1.0 / 5);
-        fd[1] = (float)(8.0 / 5); fd[0] = (float)(-205.0 / 72);
-        break;
-    case 6:
-        fd[5] = (float)(8.0 / 25200); fd[4] = (float)(-125.0 / 25200);
-        fd[3] = (float)(1000.0 / 25200); fd[2] = (float)(-6000.0 / 25200);
-        fd[1] = (float)(42000.0 / 25200); fd[0] = (float)(-73766.0 / 25200);
-        break;
-    case 7: {
-        const double den = 7.820582005659452e+44;
-        fd[6] = (float)(-4.702129633040854e+40 / den); fd[5] = (float)(8.12528000589218e+41 / den);
-        fd[4] = (float)(-6.982662505061379e+42 / den); fd[3] = (float)(4.13787407707198e+43 / den);
-        fd[2] = (float)(-2.0947987515168676e+44 / den);
-        fd[1] = (float)(1.3406712009703548e+45 / den);
-        fd[0] = (float)(-2.332705821577166e+45 / den);
-        break;
-    }
-    default:
-        break;
+    case 4: copy_weights<3>(fd); break;
+    case 5: copy_weights<4>(fd); break;
+    case 6: copy_weights<5>(fd); break;
+    case 7: copy_weights<6>(fd); break;
+    default: break;
     }
 }
 

@@ -66,40 +66,53 @@ GBX_HD float gbx_from_bits(uint32_t b)
 }
 #endif
 
-// Magnitudes for which div_const's fast path is proved (given a divisor in
-// [2^-20, 2^20] that passed the host's exhaustive binade check).
-constexpr float kDivLo = 0x1p-56f;
-constexpr float kDivHi = 0x1p56f;
-// A value in [kDiv2Lo, kDiv2Hi] can be divided twice by such a divisor on
-// the fast path (the first quotient stays inside [kDivLo, kDivHi]).
-constexpr float kDiv2Lo = 0x1p-35f;
-constexpr float kDiv2Hi = 0x1p35f;
+// Magnitudes for which div_fast is proved, given a divisor in [2^-20, 2^20]
+// that passed the host's exhaustive binade check: every quotient, remainder
+// and corrected quotient stays normal (the remainder's granularity
+// ulp(q0)*ulp(y) ~ 2^-46*|x| stays above 2^-149), so the binade [1, 2)
+// scales exactly to every |x| in [kDivLo, kDivHi].
+constexpr float kDivLo = 0x1p-100f;
+constexpr float kDivHi = 0x1p100f;
+// (x / y) / y on the fast path: the first quotient stays in [kDivLo, kDivHi].
+constexpr float kDiv2Lo = 0x1p-80f;
+constexpr float kDiv2Hi = 0x1p80f;
+
+GBX_HD float gbx_copysign(float mag, float sgn)
+{
+    return gbx_from_bits((gbx_bits(mag) & 0x7FFFFFFFu) | (gbx_bits(sgn) & 0x80000000u));
+}
 
 // Markstein's correction step with r = RN(1/y): q0 = RN(x*r) is within an
 // ulp of x/y, rem = x - q0*y is exact in one FMA, and RN(q0 + rem*r) is the
-// correctly rounded quotient.  Valid only on the proved magnitude range.
+// correctly rounded quotient.  For x = +-0 the steps give +0; the sign of
+// x/y (y > 0) is the sign of x, so it is copied back, which makes zeros exact
+// too.  Valid for x = 0 and kDivLo <= |x| <= kDivHi.
 GBX_HD float div_fast(float x, float y, float r)
 {
     const float q0 = gbx_mul(x, r);
     const float rem = gbx_fma(-q0, y, x);
-    return gbx_fma(rem, r, q0);
+    return gbx_copysign(gbx_fma(rem, r, q0), x);
+}
+
+// True when v is zero or lo <= |v| <= hi (NaN: false).
+GBX_HD bool in_fast_range(float v, float lo, float hi)
+{
+    const float a = std::fabs(v);
+    return (a <= hi) & ((a >= lo) | (a == 0.0f));
 }
 
 // x / y correctly rounded for every x (y > 0): the fast path on its proved
-// range, zeros with their sign, anything else by IEEE division.
+// range, anything else by IEEE division.
 GBX_HD float div_const(float x, float y, float r, int fast)
 {
-    const float ax = std::fabs(x);
-    if (fast && ax >= kDivLo && ax <= kDivHi) return div_fast(x, y, r);
-    if (x == 0.0f) return x;
+    if (fast && in_fast_range(x, kDivLo, kDivHi)) return div_fast(x, y, r);
     return gbx_div(x, y);
 }
 
 // (x / y) / y correctly rounded at each division.
 GBX_HD float div_const2(float x, float y, float r, int fast)
 {
-    const float ax = std::fabs(x);
-    if (fast && ax >= kDiv2Lo && ax <= kDiv2Hi) return div_fast(div_fast(x, y, r), y, r);
+    if (fast && in_fast_range(x, kDiv2Lo, kDiv2Hi)) return div_fast(div_fast(x, y, r), y, r);
     return div_const(div_const(x, y, r, fast), y, r, fast);
 }
 

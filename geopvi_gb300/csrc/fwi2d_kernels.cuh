@@ -39,6 +39,33 @@ constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 
 constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
 constexpr int kThreads = kTileX * kWarps;   // 128
 
+// Second-derivative weights of fd_coefficient (fdtd2D_modelling.c:1292-1325)
+// for half-width H = Lc-1: the reference's double literals rounded to float,
+// as compile-time constants (with m known at compile time they become
+// instruction immediates).
+template <int H>
+__host__ __device__ constexpr float fd_weight(int m)
+{
+    if (H == 3) {
+        return m == 0 ? (float)(-49.0 / 18) : m == 1 ? 1.5f : m == 2 ? (float)(-3.0 / 20) : (float)(1.0 / 90);
+    } else if (H == 4) {
+        return m == 0 ? (float)(-205.0 / 72) : m == 1 ? (float)(8.0 / 5) : m == 2 ? (float)(-1.0 / 5)
+               : m == 3 ? (float)(8.0 / 315) : (float)(-1.0 / 560);
+    } else if (H == 5) {
+        return m == 0 ? (float)(-73766.0 / 25200) : m == 1 ? (float)(42000.0 / 25200)
+               : m == 2 ? (float)(-6000.0 / 25200) : m == 3 ? (float)(1000.0 / 25200)
+               : m == 4 ? (float)(-125.0 / 25200) : (float)(8.0 / 25200);
+    } else {
+        return m == 0 ? (float)(-2.332705821577166e+45 / 7.820582005659452e+44)
+               : m == 1 ? (float)(1.3406712009703548e+45 / 7.820582005659452e+44)
+               : m == 2 ? (float)(-2.0947987515168676e+44 / 7.820582005659452e+44)
+               : m == 3 ? (float)(4.13787407707198e+43 / 7.820582005659452e+44)
+               : m == 4 ? (float)(-6.982662505061379e+42 / 7.820582005659452e+44)
+               : m == 5 ? (float)(8.12528000589218e+41 / 7.820582005659452e+44)
+                        : (float)(-4.702129633040854e+40 / 7.820582005659452e+44);
+    }
+}
+
 // Geometry shared by every solve of one launch (one parameter set).
 struct Geom {
     int ntx, ntz;        // padded grid (fdtd2D_modelling.c:86-87)
@@ -196,8 +223,7 @@ struct TileShape {
 // covers the four divisions of a cell, the rare rest takes div_const2.
 __device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Geom &g, float &ddx, float &ddz)
 {
-    const float ax = fabsf(lx), az = fabsf(lz);
-    if (g.fast_dx & g.fast_dz & (fminf(ax, az) >= kDiv2Lo) & (fmaxf(ax, az) <= kDiv2Hi)) {
+    if (g.fast_dx & g.fast_dz & in_fast_range(lx, kDiv2Lo, kDiv2Hi) & in_fast_range(lz, kDiv2Lo, kDiv2Hi)) {
         ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
         ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
     } else {
@@ -458,7 +484,7 @@ __global__ void __launch_bounds__(kThreads, 8)
     }
     float fd[H + 1];
 #pragma unroll
-    for (int m = 0; m <= H; ++m) fd[m] = g.fd[m];
+    for (int m = 0; m <= H; ++m) fd[m] = fd_weight<H>(m);
 
     // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
     const int ix0 = col0 - g.xoff;

@@ -1,12 +1,15 @@
 """Small, self-contained run of the time-step kernel for ncu captures.
 
-    python -m geopvi_gb300.profile_step --config cfg2 --solves 128 --nt 100
+    python -m geopvi_gb300.profile_step --config cfg2 --solves 140 --nt 400 --nt-interval 10
 
 Runs one misfit + gradient batch of ``solves`` (sample, shot) solves of the
 named configuration with ``nt`` shortened, all solves resident at once, no
-CUDA graph, then exits.  The wavefield state of 128 cfg2 solves (~180 MB)
-exceeds the 129 MB L2, so DRAM counters stay meaningful, while the stored
-forward field stays at a few GB.  Prints the device time of the step kernels.
+CUDA graph, then exits.  The wavefield state of 140 cfg2 solves (~200 MB)
+exceeds the 129 MB L2, so DRAM counters stay meaningful, while storing every
+10th step keeps the stored forward field near 2 GB.  A capture late in the
+run (forward launch 300, adjoint launch 699 = time index 100, both stored
+steps) sees a developed wavefield rather than the mostly-zero early field.
+Prints the device time of the step kernels.
 """
 from __future__ import annotations
 
@@ -26,9 +29,13 @@ def main():
     ap.add_argument("--solves", type=int, default=128)
     ap.add_argument("--nt", type=int, default=100)
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--nt-interval", type=int, default=None,
+                    help="store every n-th step (keeps the stored field small for multi-pass captures)")
     args = ap.parse_args()
     w = getattr(workloads, args.config)()
     p = w.params.replace(nt=args.nt)
+    if args.nt_interval:
+        p = p.replace(nt_interval=args.nt_interval)
     nsamples = max(1, -(-args.solves // p.ns))
     dev = torch.device("cuda:0")
     eng = Fwi2dEngine(p, device=dev, graph=False, max_resident=nsamples * p.ns)

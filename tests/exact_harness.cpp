@@ -21,7 +21,7 @@ long long harness_div_mismatches(float y, int klo, int khi)
     const float r = 1.0f / y;
     long long bad = 0;
     for (int k = klo; k <= khi; ++k)
-        for (uint32_t m = 0; m < (1u << 23); m += 7) {
+        for (uint32_t m = 0; m < (1u << 23); m += 97) {
             const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
             float x;
             std::memcpy(&x, &bits, 4);
@@ -31,10 +31,29 @@ long long harness_div_mismatches(float y, int klo, int khi)
             }
         }
     // zeros keep their sign; subnormals and huge values take the slow path
-    for (float xs : {0.0f, -0.0f, 1e-40f, -3e-39f, 1e30f, 3e38f}) {
+    for (float xs : {0.0f, -0.0f, 1e-40f, -3e-39f, 1e-31f, 1e30f, 3e38f}) {
         const float a = div_const(xs, y, r, 1), b = xs / y;
+        const float a2 = div_const2(xs, y, r, 1), b2 = (xs / y) / y;
         if (std::memcmp(&a, &b, 4) != 0) ++bad;
+        if (std::memcmp(&a2, &b2, 4) != 0) ++bad;
     }
+    return bad;
+}
+
+// Every significand of the binades 2^k, k in [klo, khi], through div_fast
+// directly (the proof's range ends), both signs.
+long long harness_div_fast_binades(float y, int klo, int khi)
+{
+    const float r = 1.0f / y;
+    long long bad = 0;
+    for (int k = klo; k <= khi; ++k)
+        for (uint32_t m = 0; m < (1u << 23); ++m) {
+            const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
+            float x;
+            std::memcpy(&x, &bits, 4);
+            if (div_fast(x, y, r) != x / y) ++bad;
+            if (div_fast(-x, y, r) != -x / y) ++bad;
+        }
     return bad;
 }
 

@@ -23,6 +23,8 @@ def harness(tmp_path_factory):
     L = ctypes.CDLL(out)
     L.harness_div_mismatches.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
     L.harness_div_mismatches.restype = ctypes.c_longlong
+    L.harness_div_fast_binades.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
+    L.harness_div_fast_binades.restype = ctypes.c_longlong
     L.harness_blend_mismatches.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
                                            ctypes.POINTER(ctypes.c_longlong)]
     L.harness_blend_mismatches.restype = ctypes.c_longlong
@@ -31,7 +33,14 @@ def harness(tmp_path_factory):
 
 @pytest.mark.parametrize("y", [10.0, 12.0, 9.0, 20.0, 1e-3, 2e-3, 8e-4])
 def test_division_by_grid_constants_is_correctly_rounded(harness, y):
-    assert harness.harness_div_mismatches(y, -40, 40) == 0
+    assert harness.harness_div_mismatches(y, -105, 105) == 0
+
+
+@pytest.mark.parametrize("y", [10.0, 12.0, 1e-3, 8e-4, 2.0 ** -20, 2.0 ** 20])
+def test_fast_quotient_at_the_ends_of_its_range(harness, y):
+    # the fast path's proved range is 2^-100 <= |x| <= 2^100 (binades -100 and 99 are its ends)
+    assert harness.harness_div_fast_binades(y, -100, -99) == 0
+    assert harness.harness_div_fast_binades(y, 98, 99) == 0
 
 
 @pytest.mark.parametrize("pml0", [1, 5, 10, 20, 30])
