@@ -101,11 +101,22 @@ GBX_HD bool in_fast_range(float v, float lo, float hi)
     return (a <= hi) & ((a >= lo) | (a == 0.0f));
 }
 
-// x / y correctly rounded for every x (y > 0): the fast path on its proved
-// range, anything else by IEEE division.
+// x / y correctly rounded for every x (y > 0).  On the proved range: the
+// fast path.  Below it (|x| < 2^-100, including subnormals): x * 2^64 is
+// exact and lands inside the range, and scaling the quotient back by 2^-64
+// is exact whenever the result is normal, |q * 2^-64| >= 2^-126; only
+// quotients in the subnormal range, and huge or non-finite x, take IEEE
+// division.
 GBX_HD float div_const(float x, float y, float r, int fast)
 {
-    if (fast && in_fast_range(x, kDivLo, kDivHi)) return div_fast(x, y, r);
+    if (fast) {
+        const float ax = std::fabs(x);
+        if (in_fast_range(x, kDivLo, kDivHi)) return div_fast(x, y, r);
+        if (ax < kDivLo) {
+            const float qs = div_fast(gbx_mul(x, 0x1p64f), y, r);
+            if (std::fabs(qs) >= 0x1p-62f) return gbx_mul(qs, 0x1p-64f);
+        }
+    }
     return gbx_div(x, y);
 }
 

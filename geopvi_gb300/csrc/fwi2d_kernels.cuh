@@ -246,13 +246,55 @@ struct WarpCtx {
     int inst, sample, shot;
 };
 
+// One interior row of a warp whose 32 lanes are all live: the stencil, the
+// exact quotients, the new level and the snapshot (forward) or gradient
+// term (adjoint).  The exact-quotient range tests are warp votes, so the
+// common case is one uniform branch; lanes outside the fast range (zeros
+// and tiny tails included in div_const2's scaling) fix their quotients.
+template <int H, bool ADJ>
+__device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const float (&win)[2 * H + 1],
+                                         const float *srow, float p0c, float vd, float *p2, float *ps, float *G)
+{
+    const float p1c = win[H];
+    float lx = fm(fd_weight<H>(0), p1c);
+    float lz = lx;
+#pragma unroll
+    for (int m = 1; m <= H; ++m) {
+        lx = fa(lx, fm(fd_weight<H>(m), fa(srow[m], srow[-m])));
+        lz = fa(lz, fm(fd_weight<H>(m), fa(win[H + m], win[H - m])));
+    }
+    const bool ok = (g.fast_dx & g.fast_dz) && in_fast_range(lx, kDiv2Lo, kDiv2Hi) &&
+                    in_fast_range(lz, kDiv2Lo, kDiv2Hi);
+    float ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
+    float ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
+    if (!__all_sync(0xffffffffu, ok) && !ok) {
+        ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
+    }
+    const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
+    *p2 = q;
+    if (ps) {
+        if (!ADJ) {
+            float v = q;
+            if (!b.imaging) {
+                const float x = fa(fs(q, fm(2.0f, p1c)), p0c);
+                const bool okt = g.fast_dt && in_fast_range(x, kDiv2Lo, kDiv2Hi);
+                v = div_fast(div_fast(x, g.dt, g.rdt), g.dt, g.rdt);
+                if (!__all_sync(0xffffffffu, okt) && !okt) v = div_const2(x, g.dt, g.rdt, g.fast_dt);
+            }
+            *ps = v;
+        } else {
+            *G = fa(*G, fm(*ps, q));
+        }
+    }
+}
+
 // Interior sweep: every cell of the warp is inside the interior of the
 // padded grid, away from the absorbing strips, the source and the receivers,
-// so each row is the stencil, the exact quotients, the new level and the
-// snapshot / gradient term, without per-cell region tests.
+// so each row is lean_row without per-cell region tests.
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                               const float (&fd)[H + 1], float p0_next, float vd_next)
+                                               float p0_next, float vd_next)
 {
     float win[2 * H + 1];
 #pragma unroll
@@ -272,24 +314,9 @@ __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, co
             p0_next = __ldg(p0);
             vd_next = __ldg(vdt);
         }
-        const float p1c = win[H];
-        float lx = fm(fd[0], p1c);
-        float lz = lx;
-#pragma unroll
-        for (int m = 1; m <= H; ++m) {
-            lx = fa(lx, fm(fd[m], fa(srow[m], srow[-m])));
-            lz = fa(lz, fm(fd[m], fa(win[H + m], win[H - m])));
-        }
-        float ddx, ddz;
-        laplacian_quotients(lx, lz, g, ddx, ddz);
-        const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
-        *p2 = q;
+        lean_row<H, ADJ>(g, b, win, srow, p0c, vd, p2, ps, G);
         p2 += g.pitch;
         if (ps) {
-            if (!ADJ)
-                *ps = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
-            else
-                *G = fa(*G, fm(*ps, q));
             ps += g.ipitch;
             if (ADJ) G += g.ipitch;
         }
@@ -305,7 +332,7 @@ __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, co
 // test of the reference's loops.
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                           const float (&fd)[H + 1], float p0_next, float vd_next)
+                                              bool cols_interior, float p0_next, float vd_next)
 {
     const int ix = w.ix;
     const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
@@ -336,14 +363,27 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
         }
         const float p1c = win[H];
         const int srow1 = (rr + H) * kBoxX;
+        // Rows of a warp whose columns are all interior, away from the strips,
+        // the source row and the receiver row, take the lean body (uniform test).
+        if (cols_interior && iz >= g.pml && iz < g.ntz - g.pml && iz != g.s_iz && iz != g.r_iz) {
+            float *ps = w.ps ? w.ps + (long long)(iz - g.pml) * g.ipitch : nullptr;
+            float *G = w.G ? w.G + (long long)(iz - g.pml) * g.ipitch : nullptr;
+            lean_row<H, ADJ>(g, b, win, s1 + srow1 + cx, p0c, vd, w.p2 + c, ps, G);
+            if (j + 1 < kWarpRows) {
+#pragma unroll
+                for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+                win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
+            }
+            continue;
+        }
         float q = p1c;  // cells the stencil skips keep the previous level
         if (sx && iz >= g.Lc && iz < g.ntz - g.Lc) {
-            float lx = fm(fd[0], p1c);
+            float lx = fm(fd_weight<H>(0), p1c);
             float lz = lx;
 #pragma unroll
             for (int m = 1; m <= H; ++m) {
-                lx = fa(lx, fm(fd[m], fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
-                lz = fa(lz, fm(fd[m], fa(win[H + m], win[H - m])));
+                lx = fa(lx, fm(fd_weight<H>(m), fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
+                lz = fa(lz, fm(fd_weight<H>(m), fa(win[H + m], win[H - m])));
             }
             float ddx, ddz;
             laplacian_quotients(lx, lz, g, ddx, ddz);
@@ -413,7 +453,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // per block.  Each warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads, 8)
+__global__ void __launch_bounds__(kThreads, 7)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
@@ -482,19 +522,16 @@ __global__ void __launch_bounds__(kThreads, 8)
         w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml);
         if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml);
     }
-    float fd[H + 1];
-#pragma unroll
-    for (int m = 0; m <= H; ++m) fd[m] = fd_weight<H>(m);
-
     // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
     const int ix0 = col0 - g.xoff;
-    const bool interior = w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml && ix0 >= g.pml &&
-                          ix0 + kTileX <= g.ntx - g.pml && (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
+    const bool cols_interior = ix0 >= g.pml && ix0 + kTileX <= g.ntx - g.pml;
+    const bool interior = cols_interior && w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml &&
+                          (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
                           (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
     if (interior)
-        sweep_interior<H, ADJ>(g, b, sa, w, fd, p0_next, vd_next);
+        sweep_interior<H, ADJ>(g, b, sa, w, p0_next, vd_next);
     else
-        sweep_general<H, ADJ>(g, b, sa, w, fd, p0_next, vd_next);
+        sweep_general<H, ADJ>(g, b, sa, w, cols_interior, p0_next, vd_next);
 }
 
 }  // namespace gbfwi

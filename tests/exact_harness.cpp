@@ -31,6 +31,25 @@ long long harness_div_mismatches(float y, int klo, int khi)
             }
         }
     // zeros keep their sign; subnormals and huge values take the slow path
+    // tiny magnitudes: every significand of binades near and below 2^-100
+    for (int k = -126; k <= -100; k += 2)
+        for (uint32_t m = 0; m < (1u << 23); m += 61) {
+            const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
+            float x;
+            std::memcpy(&x, &bits, 4);
+            for (float xs : {x, -x}) {
+                const float a = div_const(xs, y, r, 1), b = xs / y;
+                const float a2 = div_const2(xs, y, r, 1), b2 = (xs / y) / y;
+                if (std::memcmp(&a, &b, 4) != 0) ++bad;
+                if (std::memcmp(&a2, &b2, 4) != 0) ++bad;
+            }
+        }
+    for (uint32_t sub = 1; sub < (1u << 23); sub += 37) {  // subnormals
+        float x;
+        std::memcpy(&x, &sub, 4);
+        const float a = div_const(x, y, r, 1), b = x / y;
+        if (std::memcmp(&a, &b, 4) != 0) ++bad;
+    }
     for (float xs : {0.0f, -0.0f, 1e-40f, -3e-39f, 1e-31f, 1e30f, 3e38f}) {
         const float a = div_const(xs, y, r, 1), b = xs / y;
         const float a2 = div_const2(xs, y, r, 1), b2 = (xs / y) / y;
