@@ -29,11 +29,18 @@ def main():
     ap.add_argument("--solves", type=int, default=128)
     ap.add_argument("--nt", type=int, default=100)
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--nz", type=int, default=None, help="override the grid (acquisition re-derived)")
+    ap.add_argument("--nx", type=int, default=None)
+    ap.add_argument("--ns", type=int, default=None)
     ap.add_argument("--nt-interval", type=int, default=None,
                     help="store every n-th step (keeps the stored field small for multi-pass captures)")
     args = ap.parse_args()
     w = getattr(workloads, args.config)()
     p = w.params.replace(nt=args.nt)
+    if args.nz or args.nx or args.ns:
+        p = workloads.scaled(p, nz=args.nz, nx=args.nx, ns=args.ns)
+        base = workloads.smooth(np.ones((p.nz, p.nx)) * 2500.0 + np.linspace(0, 1500, p.nz)[:, None])
+        w.samples = np.stack([base.ravel().astype(np.float32)] * w.samples.shape[0])
     if args.nt_interval:
         p = p.replace(nt_interval=args.nt_interval)
     nsamples = max(1, -(-args.solves // p.ns))
