@@ -159,11 +159,11 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.ntz = p.nz + 2 * g.pml;
     g.ntx = p.nx + 2 * g.pml;
     // Column offset so that the interior (ix = pml) starts on a 128-byte line.
-    g.xoff = (kAlignX - g.pml % kAlignX) % kAlignX;
-    g.pitch = round_up(g.xoff + g.ntx, kAlignX);
+    g.xoff = (kTileX - g.pml % kTileX) % kTileX;
+    g.pitch = round_up(g.xoff + g.ntx, kTileX);
     g.nx = p.nx;
     g.nz = p.nz;
-    g.ipitch = round_up(p.nx, kAlignX);
+    g.ipitch = round_up(p.nx, kTileX);
     g.s_iz = g.pml + p.depths;
     g.r_iz = g.pml + p.depthr;
     g.r_ix0 = g.pml + p.nr0;
@@ -175,7 +175,7 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.nt = p.nt;
     g.nti = p.nt_interval;
     g.nt_save = p.nt / p.nt_interval + ((p.nt % p.nt_interval) ? 1 : 0);
-    g.tiles_x = (g.pitch + kTileX - 1) / kTileX;
+    g.tiles_x = g.pitch / kTileX;
     g.tiles_z = (g.ntz + kTileZ - 1) / kTileZ;
     g.fstride = (long long)g.ntz * g.pitch;
     g.pstride = (long long)g.nz * g.ipitch;

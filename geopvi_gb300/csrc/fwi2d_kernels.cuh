@@ -8,15 +8,13 @@
 // zero-lag imaging/gradient term (backward_IO, :941-978).  updata_p's copies
 // (:1053-1066) become a rotation of three buffers, so no step copies a field.
 //
-// Data movement: one block owns a 64-column x 64-row tile of one solve.  An
+// Data movement: one block owns a 32-column x 64-row tile of one solve.  An
 // elected thread stages the previous time level with its stencil halo into
 // shared memory with one TMA tensor load completing on an mbarrier; each
-// warp then sweeps 16 rows of the 64 columns, two adjacent columns per
-// thread, keeping the z-stencil windows in registers, reading x-neighbours
-// as 8-byte shared-memory pairs, the level before (p0) and v*dt with
-// coalesced 8-byte loads, and writing the new level, the stored snapshot
-// (forward) or the gradient accumulator (adjoint) with coalesced 8-byte
-// stores.
+// warp then sweeps 16 rows of its 32 columns, keeping the z-stencil window in
+// registers, reading the level before (p0) and v*dt with coalesced loads, and
+// writes the new level, the stored snapshot (forward) or the gradient
+// accumulator (adjoint) with coalesced 128-byte row stores.
 //
 // Arithmetic follows the reference operation by operation: __fmul_rn /
 // __fadd_rn / __fsub_rn never contract into FMA; divisions by the constant
@@ -33,15 +31,13 @@
 
 namespace gbfwi {
 
-constexpr int kColsPerThread = 2;  // adjacent columns per thread
-constexpr int kTileX = 32 * kColsPerThread;  // columns per tile: one warp wide
+constexpr int kTileX = 32;    // columns per tile: one warp
 constexpr int kWarpRows = 16; // rows each warp sweeps
 constexpr int kWarps = 4;     // warps per block, stacked in z
 constexpr int kTileZ = kWarpRows * kWarps;  // 64 rows per tile
 constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 16-byte aligned)
-constexpr int kBoxX = kTileX + 2 * kHaloX;  // 80 staged columns
-constexpr int kThreads = 32 * kWarps;       // 128
-constexpr int kAlignX = 32;   // the interior's first column sits on a 128-byte line
+constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
+constexpr int kThreads = kTileX * kWarps;   // 128
 
 // Second-derivative weights of fd_coefficient (fdtd2D_modelling.c:1292-1325)
 // for half-width H = Lc-1: the reference's double literals rounded to float,
@@ -215,6 +211,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+template <int H>
+struct TileShape {
+    static constexpr int kP1Rows = kTileZ + 2 * H;   // p1 rows staged
+    static constexpr int kP1Floats = kP1Rows * kBoxX;
+    static constexpr int kBytes = 4 * kP1Floats;     // TMA bytes per block
+    static constexpr int kSmem = kBytes + 16;        // + the mbarrier
+};
 
 // Exact two-step quotients (x/d)/d for both Laplacian terms; one range test
 // covers the four divisions of a cell, the rare rest takes div_const2.
@@ -229,198 +232,73 @@ __device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Ge
     }
 }
 
-// Per-thread view of one step: where the thread's two columns of 16 rows
-// live and which buffers they read and write.
+// Per-warp view of one step: where the warp's 16 x 32 cells live and which
+// buffers they read and write.
 struct WarpCtx {
-    const float *s1;             // staged p1 tile (80 columns x (64 + 2H) rows)
+    const float *s1;             // staged p1 tile (48 columns x (64 + 2H) rows)
     const float *p0;             // previous-previous level, padded field
     float *p2;                   // new level, padded field
     const float *vdt;            // v*dt, padded field
-    float *ps;                   // this thread's stored snapshot (first column), or null
-    float *G;                    // this thread's gradient accumulator (adjoint), or null
-    long long c;                 // field offset of the thread's first cell
-    int rr0, iz0, ix, cx, lane;  // first tile row, first padded row, first column, staged column, lane
+    float *ps;                   // this column's stored snapshot (interior), or null
+    float *G;                    // this column's gradient accumulator (adjoint), or null
+    long long c;                 // field offset of the warp's first cell of this lane
+    int rr0, iz0, ix, cx, lane;  // first tile row, first padded row, column, staged column, lane
     int inst, sample, shot;
 };
 
-__device__ __forceinline__ float2 ld2_shared(const float *p) { return *reinterpret_cast<const float2 *>(p); }
-__device__ __forceinline__ float2 ld2_global(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
-__device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
-
-// Laplacian numerator of one cell: fd0*p + sum fd[m]*(p[+m] + p[-m]) per
-// axis, accumulated in the reference's order (fdtd2D_modelling.c:768-774).
-// xs[H + d] holds the row value at x offset d; z offsets come from win.
-template <int H>
-__device__ __forceinline__ void laplacian_terms(const float *xs, const float (&win)[2 * H + 1], float &lx, float &lz)
+// One interior row of a warp whose 32 lanes are all live: the stencil, the
+// exact quotients, the new level and the snapshot (forward) or gradient
+// term (adjoint).  The exact-quotient range tests are warp votes, so the
+// common case is one uniform branch; lanes outside the fast range (zeros
+// and tiny tails included in div_const2's scaling) fix their quotients.
+template <int H, bool ADJ>
+__device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const float (&win)[2 * H + 1],
+                                         const float *srow, float p0c, float vd, float *p2, float *ps, float *G)
 {
-    const float p = win[H];
-    lx = fm(fd_weight<H>(0), p);
-    lz = lx;
+    const float p1c = win[H];
+    float lx = fm(fd_weight<H>(0), p1c);
+    float lz = lx;
 #pragma unroll
     for (int m = 1; m <= H; ++m) {
-        lx = fa(lx, fm(fd_weight<H>(m), fa(xs[H + m], xs[H - m])));
+        lx = fa(lx, fm(fd_weight<H>(m), fa(srow[m], srow[-m])));
         lz = fa(lz, fm(fd_weight<H>(m), fa(win[H + m], win[H - m])));
     }
-}
-
-// Two interior cells of a row (columns c and c+1), for a warp whose lanes
-// are all live and whose cells are all interior: the stencil, the exact
-// quotients, the new level and the snapshot (forward) or gradient term
-// (adjoint).  The exact-quotient range tests are warp votes, so the common
-// case is one uniform branch.
-template <int H, bool ADJ>
-__device__ __forceinline__ void lean_row2(const Geom &g, const Batch &b, const float (&wa)[2 * H + 1],
-                                          const float (&wb)[2 * H + 1], const float *srow, float2 p0c, float2 vd,
-                                          float *p2, float *ps, float *G)
-{
-    constexpr int HP = (H + 1) / 2;  // x pairs on each side
-    float xr[2 * (2 * HP + 1)];      // row values at x offsets -2HP .. 2HP+1
-#pragma unroll
-    for (int k = -HP; k <= HP; ++k) {
-        const float2 v = ld2_shared(srow + 2 * k);
-        xr[2 * (k + HP)] = v.x;
-        xr[2 * (k + HP) + 1] = v.y;
-    }
-    float lxa, lza, lxb, lzb;
-    laplacian_terms<H>(xr + 2 * HP - H, wa, lxa, lza);      // column c: offset d at xr[2HP + d]
-    laplacian_terms<H>(xr + 2 * HP + 1 - H, wb, lxb, lzb);  // column c+1
-    const bool ok = (g.fast_dx & g.fast_dz) && in_fast_range(lxa, kDiv2Lo, kDiv2Hi) &&
-                    in_fast_range(lza, kDiv2Lo, kDiv2Hi) && in_fast_range(lxb, kDiv2Lo, kDiv2Hi) &&
-                    in_fast_range(lzb, kDiv2Lo, kDiv2Hi);
-    float dxa = div_fast(div_fast(lxa, g.dx, g.rdx), g.dx, g.rdx);
-    float dza = div_fast(div_fast(lza, g.dz, g.rdz), g.dz, g.rdz);
-    float dxb = div_fast(div_fast(lxb, g.dx, g.rdx), g.dx, g.rdx);
-    float dzb = div_fast(div_fast(lzb, g.dz, g.rdz), g.dz, g.rdz);
+    const bool ok = (g.fast_dx & g.fast_dz) && in_fast_range(lx, kDiv2Lo, kDiv2Hi) &&
+                    in_fast_range(lz, kDiv2Lo, kDiv2Hi);
+    float ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
+    float ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
     if (!__all_sync(0xffffffffu, ok) && !ok) {
-        dxa = div_const2(lxa, g.dx, g.rdx, g.fast_dx);
-        dza = div_const2(lza, g.dz, g.rdz, g.fast_dz);
-        dxb = div_const2(lxb, g.dx, g.rdx, g.fast_dx);
-        dzb = div_const2(lzb, g.dz, g.rdz, g.fast_dz);
+        ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
     }
-    const float pa = wa[H], pb = wb[H];
-    const float qa = fa(fs(fm(2.0f, pa), p0c.x), fm(fm(vd.x, vd.x), fa(dxa, dza)));
-    const float qb = fa(fs(fm(2.0f, pb), p0c.y), fm(fm(vd.y, vd.y), fa(dxb, dzb)));
-    st2(p2, qa, qb);
+    const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
+    *p2 = q;
     if (ps) {
         if (!ADJ) {
-            float va = qa, vb = qb;
+            float v = q;
             if (!b.imaging) {
-                const float xa = fa(fs(qa, fm(2.0f, pa)), p0c.x);
-                const float xb = fa(fs(qb, fm(2.0f, pb)), p0c.y);
-                const bool okt = g.fast_dt && in_fast_range(xa, kDiv2Lo, kDiv2Hi) && in_fast_range(xb, kDiv2Lo, kDiv2Hi);
-                va = div_fast(div_fast(xa, g.dt, g.rdt), g.dt, g.rdt);
-                vb = div_fast(div_fast(xb, g.dt, g.rdt), g.dt, g.rdt);
-                if (!__all_sync(0xffffffffu, okt) && !okt) {
-                    va = div_const2(xa, g.dt, g.rdt, g.fast_dt);
-                    vb = div_const2(xb, g.dt, g.rdt, g.fast_dt);
-                }
+                const float x = fa(fs(q, fm(2.0f, p1c)), p0c);
+                const bool okt = g.fast_dt && in_fast_range(x, kDiv2Lo, kDiv2Hi);
+                v = div_fast(div_fast(x, g.dt, g.rdt), g.dt, g.rdt);
+                if (!__all_sync(0xffffffffu, okt) && !okt) v = div_const2(x, g.dt, g.rdt, g.fast_dt);
             }
-            st2(ps, va, vb);
+            *ps = v;
         } else {
-            const float2 gv = *reinterpret_cast<const float2 *>(G);
-            const float2 sv = *reinterpret_cast<const float2 *>(ps);
-            st2(G, fa(gv.x, fm(sv.x, qa)), fa(gv.y, fm(sv.y, qb)));
-        }
-    }
-}
-
-// One general cell: every region test of the reference's loops, the
-// absorbing-boundary blends, source injection, receiver sampling and
-// residual injection.  z-neighbours are read from the staged tile.
-template <int H, bool ADJ>
-__device__ __forceinline__ void general_cell(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                             int iz, int rr, int ix, int cx, long long c, float p0c, float vd)
-{
-    const float *s1 = w.s1;
-    const float *p0 = w.p0;
-    const int srow1 = (rr + H) * kBoxX;
-    const float p1c = s1[srow1 + cx];
-    float q = p1c;  // cells the stencil skips keep the previous level
-    if (ix >= g.Lc && ix < g.ntx - g.Lc && iz >= g.Lc && iz < g.ntz - g.Lc) {
-        float lx = fm(fd_weight<H>(0), p1c);
-        float lz = lx;
-#pragma unroll
-        for (int m = 1; m <= H; ++m) {
-            lx = fa(lx, fm(fd_weight<H>(m), fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
-            lz = fa(lz, fm(fd_weight<H>(m), fa(s1[srow1 + m * kBoxX + cx], s1[srow1 - m * kBoxX + cx])));
-        }
-        const float ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
-        const float ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
-        q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
-    }
-    const bool top = iz >= g.Lc && iz < g.pml;
-    const bool bot = iz >= g.ntz - g.pml && iz < g.ntz - g.Lc;
-    const bool lef = ix >= g.Lc && ix < g.pml;
-    const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
-    if (top || bot || lef || rig) {
-        const float s = div_const(vd, g.dx, g.rdx, g.fast_dx);
-        const float t11 = fm(fm(fs(2.0f, s), fs(1.0f, s)), 0.5f);
-        const float t12 = fm(s, fs(2.0f, s));
-        const float t13 = fm(fm(s, fs(s, 1.0f)), 0.5f);
-        if (top || bot) {  // abc_for_p top / bottom passes (fdtd2D_modelling.c:837-867)
-            const int d = top ? 1 : -1;
-            const long long st = top ? g.pitch : -(long long)g.pitch;
-            const int wi = top ? iz - g.Lc : g.ntz - g.Lc - iz - 1;
-            q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + d * kBoxX + cx], s1[srow1 + 2 * d * kBoxX + cx], p0c,
-                          __ldg(p0 + c + st), __ldg(p0 + c + 2 * st), __ldg(p0 + c + 3 * st),
-                          __ldg(p0 + c + 4 * st), b.coef[wi], b.blend_fp32);
-        }
-        if (lef || rig) {  // left / right passes (:869-899), after top / bottom
-            const int d = lef ? 1 : -1;
-            const int wi = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
-            q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + d], s1[srow1 + cx + 2 * d], p0c,
-                          __ldg(p0 + c + d), __ldg(p0 + c + 2 * d), __ldg(p0 + c + 3 * d), __ldg(p0 + c + 4 * d),
-                          b.coef[wi], b.blend_fp32);
-        }
-    }
-    if (!ADJ) {
-        if (iz == g.s_iz && ix == g.s_ix0 + w.shot * g.ds) {  // forward_IO source injection (:910)
-            const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
-            q = fa(q, fm(fm(fm(fm(sa.rik, g.dt), g.dt), v), v));
-        }
-    } else if (iz == g.r_iz) {  // backward_IO residual injection (:949-959)
-        const int ir = receiver_of(g, ix);
-        if (ir >= 0) {
-            const long long rec = ((long long)w.inst * g.nt + sa.it) * g.nr + ir;
-            const float o = b.obs[((long long)w.shot * g.nt + sa.it) * g.nr + ir];
-            const float r = b.imaging ? o : fs(b.syn[rec], o);
-            const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
-            q = fa(q, fm(fm(fm(fm(r, g.dt), g.dt), v), v));
-        }
-    }
-    w.p2[c] = q;
-    if (!ADJ && iz == g.r_iz) {  // forward_IO receiver sampling (:930-938)
-        const int ir = receiver_of(g, ix);
-        if (ir >= 0) b.syn[((long long)w.inst * g.nt + sa.it) * g.nr + ir] = q;
-    }
-    const bool inner = ix >= g.pml && ix < g.ntx - g.pml && iz >= g.pml && iz < g.ntz - g.pml;
-    if (inner && sa.snap >= 0 && (ADJ || b.store)) {
-        const long long pc = (long long)(iz - g.pml) * g.ipitch + (ix - g.pml);
-        float *ps = b.psave + ((long long)blockIdx.y * g.nt_save + sa.snap) * g.pstride + pc;
-        if (!ADJ) {
-            *ps = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
-        } else {
-            float *G = b.gacc + (long long)w.inst * g.pstride + pc;
             *G = fa(*G, fm(*ps, q));
         }
     }
 }
 
-// Interior sweep: both columns of every lane of the warp are inside the
-// interior, away from the absorbing strips, the source and the receivers,
-// so each row is lean_row2 without per-cell region tests.  z windows for the
-// two columns slide down the staged tile in registers.
+// Interior sweep: every cell of the warp is inside the interior of the
+// padded grid, away from the absorbing strips, the source and the receivers,
+// so each row is lean_row without per-cell region tests.
 template <int H, bool ADJ>
-__device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const WarpCtx &w, float2 p0_next,
-                                               float2 vd_next)
+__device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
+                                               float p0_next, float vd_next)
 {
-    float wa[2 * H + 1], wb[2 * H + 1];
+    float win[2 * H + 1];
 #pragma unroll
-    for (int m = 0; m < 2 * H + 1; ++m) {
-        const float2 v = ld2_shared(w.s1 + (w.rr0 + m) * kBoxX + w.cx);
-        wa[m] = v.x;
-        wb[m] = v.y;
-    }
+    for (int m = 0; m < 2 * H + 1; ++m) win[m] = w.s1[(w.rr0 + m) * kBoxX + w.cx];
     const float *p0 = w.p0 + w.c;
     const float *vdt = w.vdt + w.c;
     float *p2 = w.p2 + w.c;
@@ -429,87 +307,153 @@ __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, co
     const float *srow = w.s1 + (w.rr0 + H) * kBoxX + w.cx;
 #pragma unroll 1
     for (int j = 0; j < kWarpRows; ++j) {
-        const float2 p0c = p0_next, vd = vd_next;
+        const float p0c = p0_next, vd = vd_next;
         p0 += g.pitch;
         vdt += g.pitch;
         if (j + 1 < kWarpRows) {  // rows stay inside the grid: the warp is interior
-            p0_next = ld2_global(p0);
-            vd_next = ld2_global(vdt);
+            p0_next = __ldg(p0);
+            vd_next = __ldg(vdt);
         }
-        lean_row2<H, ADJ>(g, b, wa, wb, srow, p0c, vd, p2, ps, G);
+        lean_row<H, ADJ>(g, b, win, srow, p0c, vd, p2, ps, G);
         p2 += g.pitch;
         if (ps) {
             ps += g.ipitch;
             if (ADJ) G += g.ipitch;
         }
 #pragma unroll
-        for (int m = 0; m < 2 * H; ++m) {
-            wa[m] = wa[m + 1];
-            wb[m] = wb[m + 1];
-        }
+        for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
         srow += kBoxX;
-        if (j + 1 < kWarpRows) {
-            const float2 v = ld2_shared(srow + H * kBoxX);
-            wa[2 * H] = v.x;
-            wb[2 * H] = v.y;
-        }
+        if (j + 1 < kWarpRows) win[2 * H] = srow[H * kBoxX];
     }
 }
 
 // General sweep for warps that touch the rim, an absorbing strip, the
-// source row or the receiver row.  Rows whose cells are all interior (the
-// warp's columns are interior and the row is neither the source nor the
-// receiver row) still take lean_row2; other rows run general_cell on each
-// live column.
+// source row or the receiver row: the same arithmetic with every region
+// test of the reference's loops.
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                              bool cols_interior, bool live0, bool live1)
+                                              bool cols_interior, float p0_next, float vd_next)
 {
+    const int ix = w.ix;
+    const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
+    const bool lef = ix >= g.Lc && ix < g.pml;
+    const bool rig = ix >= g.ntx - g.pml && ix < g.ntx - g.Lc;
+    const int wix = lef ? ix - g.Lc : g.ntx - g.Lc - ix - 1;
+    const bool src_col = ix == g.s_ix0 + w.shot * g.ds;
+    const int cx = w.cx;
+    const float *s1 = w.s1;
+    const float *p0 = w.p0;
+    const float *vdt = w.vdt;
+
+    float win[2 * H + 1];
+#pragma unroll
+    for (int m = 0; m < 2 * H + 1; ++m) win[m] = s1[(w.rr0 + m) * kBoxX + cx];
+
 #pragma unroll 1
     for (int j = 0; j < kWarpRows; ++j) {
         const int rr = w.rr0 + j;
         const int iz = w.iz0 + j;
         if (iz >= g.ntz) break;
         const long long c = w.c + (long long)j * g.pitch;
+        const float p0c = p0_next;
+        const float vd = vd_next;
+        if (j + 1 < kWarpRows && iz + 1 < g.ntz) {  // prefetch the next row
+            p0_next = __ldg(p0 + c + g.pitch);
+            vd_next = __ldg(vdt + c + g.pitch);
+        }
+        const float p1c = win[H];
+        const int srow1 = (rr + H) * kBoxX;
+        // Rows of a warp whose columns are all interior, away from the strips,
+        // the source row and the receiver row, take the lean body (uniform test).
         if (cols_interior && iz >= g.pml && iz < g.ntz - g.pml && iz != g.s_iz && iz != g.r_iz) {
-            float wa[2 * H + 1], wb[2 * H + 1];
-#pragma unroll
-            for (int m = 0; m < 2 * H + 1; ++m) {
-                const float2 v = ld2_shared(w.s1 + (rr + m) * kBoxX + w.cx);
-                wa[m] = v.x;
-                wb[m] = v.y;
-            }
             float *ps = w.ps ? w.ps + (long long)(iz - g.pml) * g.ipitch : nullptr;
             float *G = w.G ? w.G + (long long)(iz - g.pml) * g.ipitch : nullptr;
-            lean_row2<H, ADJ>(g, b, wa, wb, w.s1 + (rr + H) * kBoxX + w.cx, ld2_global(w.p0 + c),
-                              ld2_global(w.vdt + c), w.p2 + c, ps, G);
+            lean_row<H, ADJ>(g, b, win, s1 + srow1 + cx, p0c, vd, w.p2 + c, ps, G);
+            if (j + 1 < kWarpRows) {
+#pragma unroll
+                for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+                win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
+            }
             continue;
         }
-        if (live0)
-            general_cell<H, ADJ>(g, b, sa, w, iz, rr, w.ix, w.cx, c, __ldg(w.p0 + c), __ldg(w.vdt + c));
-        if (live1)
-            general_cell<H, ADJ>(g, b, sa, w, iz, rr, w.ix + 1, w.cx + 1, c + 1, __ldg(w.p0 + c + 1),
-                                 __ldg(w.vdt + c + 1));
+        float q = p1c;  // cells the stencil skips keep the previous level
+        if (sx && iz >= g.Lc && iz < g.ntz - g.Lc) {
+            float lx = fm(fd_weight<H>(0), p1c);
+            float lz = lx;
+#pragma unroll
+            for (int m = 1; m <= H; ++m) {
+                lx = fa(lx, fm(fd_weight<H>(m), fa(s1[srow1 + cx + m], s1[srow1 + cx - m])));
+                lz = fa(lz, fm(fd_weight<H>(m), fa(win[H + m], win[H - m])));
+            }
+            float ddx, ddz;
+            laplacian_quotients(lx, lz, g, ddx, ddz);
+            q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
+        }
+        const bool top = iz >= g.Lc && iz < g.pml;
+        const bool bot = iz >= g.ntz - g.pml && iz < g.ntz - g.Lc;
+        if (top || bot || lef || rig) {
+            const float s = div_const(vd, g.dx, g.rdx, g.fast_dx);
+            const float t11 = fm(fm(fs(2.0f, s), fs(1.0f, s)), 0.5f);
+            const float t12 = fm(s, fs(2.0f, s));
+            const float t13 = fm(fm(s, fs(s, 1.0f)), 0.5f);
+            if (top || bot) {  // abc_for_p top / bottom passes (fdtd2D_modelling.c:837-867)
+                const long long st = top ? g.pitch : -(long long)g.pitch;
+                const int wi = top ? iz - g.Lc : g.ntz - g.Lc - iz - 1;
+                q = abc_blend(q, t11, t12, t13, p1c, top ? win[H + 1] : win[H - 1], top ? win[H + 2] : win[H - 2],
+                              p0c, __ldg(p0 + c + st), __ldg(p0 + c + 2 * st), __ldg(p0 + c + 3 * st),
+                              __ldg(p0 + c + 4 * st), b.coef[wi], b.blend_fp32);
+            }
+            if (lef || rig) {  // left / right passes (:869-899), after top / bottom
+                const int d = lef ? 1 : -1;
+                q = abc_blend(q, t11, t12, t13, p1c, s1[srow1 + cx + d], s1[srow1 + cx + 2 * d], p0c,
+                              __ldg(p0 + c + d), __ldg(p0 + c + 2 * d), __ldg(p0 + c + 3 * d),
+                              __ldg(p0 + c + 4 * d), b.coef[wix], b.blend_fp32);
+            }
+        }
+        if (!ADJ) {
+            if (iz == g.s_iz && src_col) {  // forward_IO source injection (:910)
+                const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
+                q = fa(q, fm(fm(fm(fm(sa.rik, g.dt), g.dt), v), v));
+            }
+        } else if (iz == g.r_iz) {  // backward_IO residual injection (:949-959)
+            const int ir = receiver_of(g, ix);
+            if (ir >= 0) {
+                const long long rec = ((long long)w.inst * g.nt + sa.it) * g.nr + ir;
+                const float o = b.obs[((long long)w.shot * g.nt + sa.it) * g.nr + ir];
+                const float r = b.imaging ? o : fs(b.syn[rec], o);
+                const float v = padded_velocity(g, b.vel + (long long)w.sample * g.nx * g.nz, iz, ix);
+                q = fa(q, fm(fm(fm(fm(r, g.dt), g.dt), v), v));
+            }
+        }
+        w.p2[c] = q;
+        if (!ADJ && iz == g.r_iz) {  // forward_IO receiver sampling (:930-938)
+            const int ir = receiver_of(g, ix);
+            if (ir >= 0) b.syn[((long long)w.inst * g.nt + sa.it) * g.nr + ir] = q;
+        }
+        if (w.ps && iz >= g.pml && iz < g.ntz - g.pml) {
+            const long long pc = (long long)(iz - g.pml) * g.ipitch;
+            if (!ADJ)
+                w.ps[pc] = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+            else
+                w.G[pc] = fa(w.G[pc], fm(w.ps[pc], q));
+        }
+        if (j + 1 < kWarpRows) {  // slide the z window one row down
+#pragma unroll
+            for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
+            win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
+        }
     }
 }
 
-template <int H>
-struct TileShape {
-    static constexpr int kP1Rows = kTileZ + 2 * H;   // p1 rows staged
-    static constexpr int kP1Floats = kP1Rows * kBoxX;
-    static constexpr int kBytes = 4 * kP1Floats;     // TMA bytes per block
-    static constexpr int kSmem = kBytes + 16;        // + the mbarrier
-};
-
 // One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
-// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with an
-// (80, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
+// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with a
+// (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
 // and v*dt are read once per cell with coalesced read-only loads (the
-// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~23 KB
+// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
 // per block.  Each warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads, 5)
+__global__ void __launch_bounds__(kThreads, 7)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
@@ -542,32 +486,24 @@ __global__ void __launch_bounds__(kThreads, 5)
     w.shot = w.inst - w.sample * g.ns;
     w.lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int col = col0 + kColsPerThread * w.lane;
+    const int col = col0 + w.lane;
     w.ix = col - g.xoff;
-    w.cx = kColsPerThread * w.lane + kHaloX;
+    w.cx = w.lane + kHaloX;
     w.rr0 = warp * kWarpRows;
     w.iz0 = row0 + w.rr0;
     w.s1 = s1;
-    const bool live0 = w.ix >= 0 && w.ix < g.ntx;
-    const bool live1 = w.ix + 1 >= 0 && w.ix + 1 < g.ntx;
+    const bool live = w.ix >= 0 && w.ix < g.ntx;
     float *ring = b.ring + (long long)slot * 3 * g.fstride;
     w.p0 = ring + (long long)b0 * g.fstride;
     w.p2 = ring + (long long)b2 * g.fstride;
     w.vdt = b.vdt + (long long)w.sample * g.fstride;
     w.c = (long long)w.iz0 * g.pitch + col;
 
-    // Warp-uniform: all 16 rows and 64 columns interior, no source or receiver row.
-    const int ix0 = col0 - g.xoff;
-    const bool cols_interior = ix0 >= g.pml && ix0 + kTileX <= g.ntx - g.pml;
-    const bool interior = cols_interior && w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml &&
-                          (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
-                          (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
-
-    // Interior warps issue their first p0 / v*dt loads while the tile is in flight.
-    float2 p0_next = make_float2(0.0f, 0.0f), vd_next = p0_next;
-    if (interior) {
-        p0_next = ld2_global(w.p0 + w.c);
-        vd_next = ld2_global(w.vdt + w.c);
+    // Issue this thread's first p0 / v*dt loads while the tile is in flight.
+    float p0_next = 0.0f, vd_next = 0.0f;
+    if (live && w.iz0 < g.ntz) {
+        p0_next = __ldg(w.p0 + w.c);
+        vd_next = __ldg(w.vdt + w.c);
     }
 
     if (!mbar_wait_bounded(&bar, 0)) {
@@ -577,20 +513,25 @@ __global__ void __launch_bounds__(kThreads, 5)
         mbar_wait_bounded(&bar, 0);
         return;
     }
-    if (!(live0 || live1) || w.iz0 >= g.ntz) return;
+    if (!live || w.iz0 >= g.ntz) return;
 
-    // Snapshot and gradient columns (interior columns only; a pair is either
-    // both interior or handled cell by cell in general_cell).
+    const bool inner_x = w.ix >= g.pml && w.ix < g.ntx - g.pml;
     w.ps = nullptr;
     w.G = nullptr;
-    if (sa.snap >= 0 && cols_interior && (ADJ || b.store)) {
+    if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
         w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml);
         if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml);
     }
+    // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
+    const int ix0 = col0 - g.xoff;
+    const bool cols_interior = ix0 >= g.pml && ix0 + kTileX <= g.ntx - g.pml;
+    const bool interior = cols_interior && w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml &&
+                          (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
+                          (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
     if (interior)
-        sweep_interior<H, ADJ>(g, b, w, p0_next, vd_next);
+        sweep_interior<H, ADJ>(g, b, sa, w, p0_next, vd_next);
     else
-        sweep_general<H, ADJ>(g, b, sa, w, cols_interior, live0, live1);
+        sweep_general<H, ADJ>(g, b, sa, w, cols_interior, p0_next, vd_next);
 }
 
 }  // namespace gbfwi
