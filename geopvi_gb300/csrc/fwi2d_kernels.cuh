@@ -291,39 +291,59 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
 
 // Interior sweep: every cell of the warp is inside the interior of the
 // padded grid, away from the absorbing strips, the source and the receivers,
-// so each row is lean_row without per-cell region tests.
+// so each row is lean_row without per-cell region tests.  Rows go in blocks
+// of kUnroll: the z window covers the block (2H + kUnroll values), the
+// block's p0 / v*dt rows are fetched one block ahead, and the rows'
+// independent dependency chains interleave.
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                               float p0_next, float vd_next)
+                                               float p0_first, float vd_first)
 {
-    float win[2 * H + 1];
+    constexpr int U = 4;
+    static_assert(kWarpRows % U == 0, "row blocks must tile the warp's rows");
+    float win[2 * H + U];
 #pragma unroll
-    for (int m = 0; m < 2 * H + 1; ++m) win[m] = w.s1[(w.rr0 + m) * kBoxX + w.cx];
+    for (int m = 0; m < 2 * H; ++m) win[m] = w.s1[(w.rr0 + m) * kBoxX + w.cx];
+    const long long pitch = g.pitch;
     const float *p0 = w.p0 + w.c;
     const float *vdt = w.vdt + w.c;
     float *p2 = w.p2 + w.c;
     float *ps = w.ps ? w.ps + (long long)(w.iz0 - g.pml) * g.ipitch : nullptr;
     float *G = w.G ? w.G + (long long)(w.iz0 - g.pml) * g.ipitch : nullptr;
-    const float *srow = w.s1 + (w.rr0 + H) * kBoxX + w.cx;
+    const float *scol = w.s1 + w.rr0 * kBoxX + w.cx;  // staged row rr0 - H of this column
+    float p0n[U], vdn[U];
+    p0n[0] = p0_first;
+    vdn[0] = vd_first;
+#pragma unroll
+    for (int u = 1; u < U; ++u) {
+        p0n[u] = __ldg(p0 + u * pitch);
+        vdn[u] = __ldg(vdt + u * pitch);
+    }
 #pragma unroll 1
-    for (int j = 0; j < kWarpRows; ++j) {
-        const float p0c = p0_next, vd = vd_next;
-        p0 += g.pitch;
-        vdt += g.pitch;
-        if (j + 1 < kWarpRows) {  // rows stay inside the grid: the warp is interior
-            p0_next = __ldg(p0);
-            vd_next = __ldg(vdt);
+    for (int j0 = 0; j0 < kWarpRows; j0 += U) {
+        float p0c[U], vd[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            p0c[u] = p0n[u];
+            vd[u] = vdn[u];
+            win[2 * H + u] = scol[(j0 + 2 * H + u) * kBoxX];
         }
-        lean_row<H, ADJ>(g, b, win, srow, p0c, vd, p2, ps, G);
-        p2 += g.pitch;
-        if (ps) {
-            ps += g.ipitch;
-            if (ADJ) G += g.ipitch;
+        if (j0 + U < kWarpRows) {  // fetch the next block's rows (inside the grid: the warp is interior)
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                p0n[u] = __ldg(p0 + (j0 + U + u) * pitch);
+                vdn[u] = __ldg(vdt + (j0 + U + u) * pitch);
+            }
         }
 #pragma unroll
-        for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
-        srow += kBoxX;
-        if (j + 1 < kWarpRows) win[2 * H] = srow[H * kBoxX];
+        for (int u = 0; u < U; ++u) {
+            const float(&wu)[2 * H + 1] = *reinterpret_cast<const float(*)[2 * H + 1]>(win + u);
+            float *psu = ps ? ps + (long long)(j0 + u) * g.ipitch : nullptr;
+            float *Gu = (ADJ && ps) ? G + (long long)(j0 + u) * g.ipitch : nullptr;
+            lean_row<H, ADJ>(g, b, wu, scol + (j0 + u + H) * kBoxX, p0c[u], vd[u], p2 + (j0 + u) * pitch, psu, Gu);
+        }
+#pragma unroll
+        for (int m = 0; m < 2 * H; ++m) win[m] = win[m + U];
     }
 }
 
@@ -453,7 +473,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // per block.  Each warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads, 7)
+__global__ void __launch_bounds__(kThreads, 6)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
