@@ -24,8 +24,11 @@
 
 #if defined(__CUDACC__)
 #define GBX_HD __host__ __device__ __forceinline__
+// Rare paths stay out of line so the hot loops keep a small instruction footprint.
+#define GBX_COLD __host__ __device__ __noinline__
 #else
 #define GBX_HD inline
+#define GBX_COLD inline
 #endif
 
 namespace gbfwi {
@@ -107,24 +110,32 @@ GBX_HD bool in_fast_range(float v, float lo, float hi)
 // is exact whenever the result is normal, |q * 2^-64| >= 2^-126; only
 // quotients in the subnormal range, and huge or non-finite x, take IEEE
 // division.
-GBX_HD float div_const(float x, float y, float r, int fast)
+GBX_COLD float div_const_slow(float x, float y, float r, int fast)
 {
-    if (fast) {
-        const float ax = std::fabs(x);
-        if (in_fast_range(x, kDivLo, kDivHi)) return div_fast(x, y, r);
-        if (ax < kDivLo) {
-            const float qs = div_fast(gbx_mul(x, 0x1p64f), y, r);
-            if (std::fabs(qs) >= 0x1p-62f) return gbx_mul(qs, 0x1p-64f);
-        }
+    if (fast && std::fabs(x) < kDivLo) {
+        const float qs = div_fast(gbx_mul(x, 0x1p64f), y, r);
+        if (std::fabs(qs) >= 0x1p-62f) return gbx_mul(qs, 0x1p-64f);
     }
     return gbx_div(x, y);
 }
 
+GBX_HD float div_const(float x, float y, float r, int fast)
+{
+    if (fast && in_fast_range(x, kDivLo, kDivHi)) return div_fast(x, y, r);
+    return div_const_slow(x, y, r, fast);
+}
+
 // (x / y) / y correctly rounded at each division.
+GBX_COLD float div_const2_slow(float x, float y, float r, int fast)
+{
+    const float q = (fast && in_fast_range(x, kDivLo, kDivHi)) ? div_fast(x, y, r) : div_const_slow(x, y, r, fast);
+    return (fast && in_fast_range(q, kDivLo, kDivHi)) ? div_fast(q, y, r) : div_const_slow(q, y, r, fast);
+}
+
 GBX_HD float div_const2(float x, float y, float r, int fast)
 {
     if (fast && in_fast_range(x, kDiv2Lo, kDiv2Hi)) return div_fast(div_fast(x, y, r), y, r);
-    return div_const(div_const(x, y, r, fast), y, r, fast);
+    return div_const2_slow(x, y, r, fast);
 }
 
 // Split of 1 - w into floats bh + bl (exact) for the boundary blend, with
@@ -148,6 +159,8 @@ struct BlendCoef {
 // is a power of two), every value between X and RN_d(X) rounds to r, which
 // is then the reference's result.  Otherwise -- zeros aside -- the double
 // formula is evaluated (rare: near-ties, cancellation, extreme magnitudes).
+GBX_COLD float blend_mix_double(float a, float q, double omw) { return gbx_d2f(gbx_dmix(a, omw, q)); }
+
 GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
 {
     if (q == 0.0f) return gbx_add(a, gbx_mul(c.bh, q));  // a + (+-0), signs as in double
@@ -176,7 +189,7 @@ GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
             if (gbx_add(std::fabs(d), err) < gbx_mul(hu, 0.99f)) return r;
         }
     }
-    return gbx_d2f(gbx_dmix(a, c.omw, q));
+    return blend_mix_double(a, q, c.omw);
 }
 
 }  // namespace gbfwi

@@ -268,8 +268,8 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
     float ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
     float ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
     if (!__all_sync(0xffffffffu, ok) && !ok) {
-        ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
-        ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
+        ddx = div_const2_slow(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div_const2_slow(lz, g.dz, g.rdz, g.fast_dz);
     }
     const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
     *p2 = q;
@@ -280,7 +280,7 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
                 const float x = fa(fs(q, fm(2.0f, p1c)), p0c);
                 const bool okt = g.fast_dt && in_fast_range(x, kDiv2Lo, kDiv2Hi);
                 v = div_fast(div_fast(x, g.dt, g.rdt), g.dt, g.rdt);
-                if (!__all_sync(0xffffffffu, okt) && !okt) v = div_const2(x, g.dt, g.rdt, g.fast_dt);
+                if (!__all_sync(0xffffffffu, okt) && !okt) v = div_const2_slow(x, g.dt, g.rdt, g.fast_dt);
             }
             *ps = v;
         } else {
