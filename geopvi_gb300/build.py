@@ -51,6 +51,11 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _defines() -> list[str]:
+    """Build-time tuning knobs, e.g. GEOPVI_GB300_DEFINES="GB_FWI2D_MIN_BLOCKS=8"."""
+    return ["-D" + d for d in os.environ.get("GEOPVI_GB300_DEFINES", "").split() if d]
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile every .cu in csrc/ into one shared library; return its path."""
     if not force and not _stale():
@@ -61,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     procs = []
     for src in sources():
         obj = os.path.join(LIB_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", os.path.join(REPO_DIR, "include"), "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *_defines(), "-I", os.path.join(REPO_DIR, "include"), "-c", src, "-o", obj]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
         objs.append(obj)
     logs = []

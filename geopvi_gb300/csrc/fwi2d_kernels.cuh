@@ -39,6 +39,12 @@ constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 
 constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
 constexpr int kThreads = kTileX * kWarps;   // 128
 
+// Resident blocks per SM the step kernel is compiled for (register cap
+// 65536 / (128 * this)); a build-time tuning knob.
+#ifndef GB_FWI2D_MIN_BLOCKS
+#define GB_FWI2D_MIN_BLOCKS 7
+#endif
+
 // Second-derivative weights of fd_coefficient (fdtd2D_modelling.c:1292-1325)
 // for half-width H = Lc-1: the reference's double literals rounded to float,
 // as compile-time constants (with m known at compile time they become
@@ -349,10 +355,12 @@ __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, co
 
 // General sweep for warps that touch the rim, an absorbing strip, the
 // source row or the receiver row: the same arithmetic with every region
-// test of the reference's loops.
+// test of the reference's loops.  (Routing this sweep's interior rows to
+// lean_row was measured slower: the second copy of the row body costs more
+// in instruction-cache misses and registers than the region tests save.)
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
-                                              bool cols_interior, float p0_next, float vd_next)
+                                              float p0_next, float vd_next)
 {
     const int ix = w.ix;
     const bool sx = ix >= g.Lc && ix < g.ntx - g.Lc;
@@ -383,19 +391,6 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
         }
         const float p1c = win[H];
         const int srow1 = (rr + H) * kBoxX;
-        // Rows of a warp whose columns are all interior, away from the strips,
-        // the source row and the receiver row, take the lean body (uniform test).
-        if (cols_interior && iz >= g.pml && iz < g.ntz - g.pml && iz != g.s_iz && iz != g.r_iz) {
-            float *ps = w.ps ? w.ps + (long long)(iz - g.pml) * g.ipitch : nullptr;
-            float *G = w.G ? w.G + (long long)(iz - g.pml) * g.ipitch : nullptr;
-            lean_row<H, ADJ>(g, b, win, s1 + srow1 + cx, p0c, vd, w.p2 + c, ps, G);
-            if (j + 1 < kWarpRows) {
-#pragma unroll
-                for (int m = 0; m < 2 * H; ++m) win[m] = win[m + 1];
-                win[2 * H] = s1[(rr + 1 + 2 * H) * kBoxX + cx];
-            }
-            continue;
-        }
         float q = p1c;  // cells the stencil skips keep the previous level
         if (sx && iz >= g.Lc && iz < g.ntz - g.Lc) {
             float lx = fm(fd_weight<H>(0), p1c);
@@ -473,7 +468,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // per block.  Each warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads, 6)
+__global__ void __launch_bounds__(kThreads, GB_FWI2D_MIN_BLOCKS)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
@@ -551,7 +546,7 @@ __global__ void __launch_bounds__(kThreads, 6)
     if (interior)
         sweep_interior<H, ADJ>(g, b, sa, w, p0_next, vd_next);
     else
-        sweep_general<H, ADJ>(g, b, sa, w, cols_interior, p0_next, vd_next);
+        sweep_general<H, ADJ>(g, b, sa, w, p0_next, vd_next);
 }
 
 }  // namespace gbfwi
