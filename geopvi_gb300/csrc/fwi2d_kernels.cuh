@@ -42,7 +42,7 @@ constexpr int kThreads = kTileX * kWarps;   // 128
 // Resident blocks per SM the step kernel is compiled for (register cap
 // 65536 / (128 * this)); a build-time tuning knob.
 #ifndef GB_FWI2D_MIN_BLOCKS
-#define GB_FWI2D_MIN_BLOCKS 7
+#define GB_FWI2D_MIN_BLOCKS 8
 #endif
 
 // Second-derivative weights of fd_coefficient (fdtd2D_modelling.c:1292-1325)
