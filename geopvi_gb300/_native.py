@@ -18,6 +18,7 @@ FLOAT_FIELDS = ("dx", "dz", "dt", "f0")
 
 OK = 0
 ENOENT = -2
+E2BIG = -7
 ENOMEM = -12
 EINVAL = -22
 ENOTSUP = -95
@@ -32,7 +33,9 @@ FLAG_CHECKPOINT = 0x8
 FLAG_FORWARD_ONLY = 0x10
 FLAG_PROFILE = 0x20
 
-STATUS_NAMES = {ENOENT: "ENOENT (parameter file missing)", ENOMEM: "ENOMEM (device memory)",
+STATIC_SCRATCH_BYTES = 64 << 20
+
+STATUS_NAMES = {ENOENT: "ENOENT (parameter file missing)", E2BIG: "E2BIG (batch exceeds the static scratch)", ENOMEM: "ENOMEM (device memory)",
                 EINVAL: "EINVAL (invalid parameters or buffers)",
                 ENOTSUP: "ENOTSUP (pseudo-spectral Laplacian not built)",
                 ENAN: "ENAN (NaN in velocity)", ECUDA: "ECUDA (CUDA runtime error)",
@@ -43,6 +46,7 @@ EXPORTED_SYMBOLS = (
     "gb_fwi2d_read_params", "gb_fwi2d_validate", "fwi_2D", "forward_2D",
     "gb_fwi2d_workspace_bytes", "gb_fwi2d_batch", "gb_fwi2d_last_launch_count",
     "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms", "gb_fwi2d_status",
+    "gb_fwi2d_batch_noalloc",
 )
 
 
@@ -90,6 +94,9 @@ def load() -> ctypes.CDLL:
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         L.gb_fwi2d_batch.restype = ctypes.c_int
+        L.gb_fwi2d_batch_noalloc.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p]
+        L.gb_fwi2d_batch_noalloc.restype = ctypes.c_int
         L.gb_fwi2d_last_launch_count.argtypes = []
         L.gb_fwi2d_last_launch_count.restype = ctypes.c_longlong
         L.gb_fwi2d_profile_step_ms.argtypes = [ctypes.POINTER(ctypes.c_longlong)]

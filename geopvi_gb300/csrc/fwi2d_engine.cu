@@ -858,3 +858,94 @@ int forward_2D(char input_file[200], float *vel_inner, float *record_syn, int ru
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point (gb_fwi2d_batch_noalloc)
+//
+// For callers that cannot allocate device memory -- code that must not call
+// cudaMalloc or a pool allocator while it runs (a host whose device memory is
+// owned by another runtime or a fixed pool, a latency-critical loop where an
+// allocation would synchronize the device), or a plain C caller through an
+// FFI that has no way to hand over a workspace.  The workspace then lives in
+// a fixed array that this library reserves on every GPU that loads it, for
+// the life of the process.
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) unsigned char g_static_scratch[GB_FWI2D_STATIC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+void *g_static_addr[kMaxDevices] = {};
+
+// Device address of the static scratch array on the current device.  In host
+// code the array's name is only a host-side stand-in, so the address is
+// looked up once per device (with that device current) and cached.
+int static_scratch(void **out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GB_FWI2D_ECUDA;
+    std::lock_guard<std::mutex> lk(g_static_mutex);
+    if (!g_static_addr[dev]) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_static_scratch) != cudaSuccess || !ptr) return GB_FWI2D_ECUDA;
+        g_static_addr[dev] = ptr;
+    }
+    *out = g_static_addr[dev];
+    return GB_FWI2D_OK;
+}
+
+}  // namespace
+
+extern "C" int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
+                                      float *syn, float *grad, double *misfit, unsigned flags, void *stream)
+{
+    t_last_launches = 0;
+    if (!p || nsamples <= 0 || !vel || !obs) return GB_FWI2D_EINVAL;
+    if (flags & ~(GB_FWI2D_IMAGING | GB_FWI2D_FORWARD_ONLY | GB_FWI2D_PLAIN)) return GB_FWI2D_EINVAL;
+    Derived d;
+    int st = derive(*p, d);
+    if (st) return st;
+    const bool fwd_only = (flags & GB_FWI2D_FORWARD_ONLY) != 0;
+    const size_t coef_bytes = align256(sizeof(BlendCoef) * d.coef.size());
+    const size_t cap = GB_FWI2D_STATIC_SCRATCH_BYTES;
+    // Largest resident count whose workspace fits beside the weight table.
+    const long long ninst = (long long)nsamples * d.g.ns;
+    Layout L = plan_layout(d.g, nsamples, 1, syn == nullptr, fwd_only);
+    if (coef_bytes + L.total > cap) return GB_FWI2D_E2BIG;
+    long long lo = 1, hi = ninst;
+    while (lo < hi) {
+        const long long mid = (lo + hi + 1) / 2;
+        if (coef_bytes + plan_layout(d.g, nsamples, (int)mid, syn == nullptr, fwd_only).total <= cap)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    L = plan_layout(d.g, nsamples, (int)lo, syn == nullptr, fwd_only);
+    void *base = nullptr;
+    st = static_scratch(&base);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    Call c;
+    c.d = &d;
+    c.L = L;
+    c.nsamples = nsamples;
+    c.vel = vel;
+    c.obs = obs;
+    c.syn = syn;
+    c.grad = grad;
+    c.misfit = misfit;
+    c.flags = flags;
+    c.work = (char *)base + coef_bytes;
+    c.profile = false;
+    c.tab.coef = (BlendCoef *)base;
+    // The weight table is copied from pageable host memory: the copy returns
+    // once the data are staged, so the local table may go out of scope.
+    if (cudaMemcpyAsync(c.tab.coef, d.coef.data(), sizeof(BlendCoef) * d.coef.size(), cudaMemcpyHostToDevice,
+                        s) != cudaSuccess)
+        return GB_FWI2D_ECUDA;
+    if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident)) return GB_FWI2D_ECUDA;
+    const long long launches = enqueue(c, s);
+    t_last_launches = launches;
+    return cudaGetLastError() == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
+}

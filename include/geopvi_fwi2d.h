@@ -32,6 +32,7 @@ extern "C" {
 /* Status codes. */
 #define GB_FWI2D_OK 0
 #define GB_FWI2D_ENOENT (-2)     /* parameter file missing */
+#define GB_FWI2D_E2BIG (-7)      /* batch needs more than the static scratch (gb_fwi2d_batch_noalloc) */
 #define GB_FWI2D_ENOMEM (-12)    /* device memory / workspace too small */
 #define GB_FWI2D_EINVAL (-22)    /* bad geometry, sizes or pointers */
 #define GB_FWI2D_ENOTSUP (-95)   /* valid in the reference but not built here */
@@ -97,6 +98,34 @@ size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_
 int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
                    float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
                    void *work, size_t work_bytes, void *stream);
+
+/* Allocation-free variant of gb_fwi2d_batch.  No counterpart in the
+ * reference (whose solver allocates and frees its own buffers on every call).
+ *
+ * For callers that cannot allocate device memory: a host whose device memory
+ * belongs to another runtime or to a fixed pool, a latency-critical loop in
+ * which an allocation would synchronize the device, or a plain C/FFI caller
+ * with no way to provide a workspace.  Instead of a caller workspace it uses a
+ * fixed array of GB_FWI2D_STATIC_SCRATCH_BYTES that the library reserves on
+ * every GPU that loads it, until the process exits.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *
+ * Inputs and outputs are the caller's device buffers, as in gb_fwi2d_batch
+ * (syn may be NULL).  flags: GB_FWI2D_IMAGING, GB_FWI2D_FORWARD_ONLY,
+ * GB_FWI2D_PLAIN only.  The batch is split into as many waves as the scratch
+ * needs; a batch whose per-sample state alone (padded v*dt, gradient
+ * accumulators, synthetic data when syn is NULL) plus one resident solve does
+ * not fit returns GB_FWI2D_E2BIG.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  Every call shares the one array, which keeps the last call's
+ * contents (each call clears what must start at zero): calls that overlap on
+ * the GPU -- on different streams, or from different threads -- race and
+ * corrupt each other's results; serialize them. */
+#define GB_FWI2D_STATIC_SCRATCH_BYTES (64u << 20)
+int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
+                           float *syn, float *grad, double *misfit, unsigned flags, void *stream);
 
 /* Waits for `stream`, then reads the device status word at the start of a
  * workspace used by gb_fwi2d_batch: GB_FWI2D_OK, or GB_FWI2D_ETIMEOUT if a
