@@ -211,26 +211,48 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
 
 struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
+    size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
     int resident;
+    int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
 };
+
+// sqrt(nt) checkpointing: segments of K steps (K a multiple of nt_interval,
+// so every segment's stored steps are contiguous), one (p0, p1) pair kept
+// per segment.
+static void checkpoint_plan(const Geom &g, int &K, int &nseg)
+{
+    const int root = (int)std::ceil(std::sqrt((double)g.nt));
+    K = (root + g.nti - 1) / g.nti * g.nti;
+    nseg = (g.nt + K - 1) / K;
+}
 
 constexpr int kMisfitBlocks = 64;  // partial sums per sample for the misfit
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in_work,
-                          bool forward_only)
+                          bool forward_only, bool checkpoint = false)
 {
     Layout L{};
     const long long ninst = (long long)nsamples * g.ns;
     if (resident <= 0 || resident > ninst) resident = (int)ninst;
     L.resident = resident;
+    checkpoint = checkpoint && !forward_only;
+    long long snaps = g.nt_save;  // stored steps per resident solve
+    if (checkpoint) {
+        checkpoint_plan(g, L.ckpt_k, L.ckpt_nseg);
+        snaps = L.ckpt_k / g.nti;
+    }
     size_t off = 0;
     L.status = off; off = align256(off + sizeof(int));
     L.vdt = off;   off = align256(off + sizeof(float) * g.fstride * nsamples);
     L.ring = off;  off = align256(off + sizeof(float) * g.fstride * 3 * resident);
+    if (checkpoint) {
+        L.ring2 = off; off = align256(off + sizeof(float) * g.fstride * 3 * resident);
+        L.ckpt = off;  off = align256(off + sizeof(float) * g.fstride * 2 * L.ckpt_nseg * resident);
+    }
     L.psave = off;
-    if (!forward_only) off = align256(off + sizeof(float) * g.pstride * g.nt_save * resident);
+    if (!forward_only) off = align256(off + sizeof(float) * g.pstride * snaps * resident);
     L.gacc = off;
     if (!forward_only) off = align256(off + sizeof(float) * g.pstride * ninst);
     L.syn = off;
@@ -465,12 +487,104 @@ struct Call {
     char *work;
     bool profile;
     Maps maps;
+    Maps maps2;  // checkpointing: the adjoint's ring
 };
 
 static int grid_for(long long n, int threads)
 {
     long long b = (n + threads - 1) / threads;
     return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
+}
+
+// One wave with sqrt(nt) checkpointing: the forward pass keeps (p0, p1) at the
+// start of every K-step segment instead of every stored step; the adjoint then
+// walks the segments backwards, restoring each pair into the forward ring,
+// recomputing that segment's forward steps (which store its snapshots) and
+// running the segment's adjoint steps in a second ring.  The recomputation runs
+// the same kernel on the same inputs, so the snapshots -- and the gradient --
+// are bit for bit those of full storage.
+static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStream_t st)
+{
+    Geom g = c.d->g;
+    const int K = c.L.ckpt_k, nseg = c.L.ckpt_nseg;
+    g.nt_save = K / g.nti;  // snapshot slots per resident solve: one segment's
+    float *ring = (float *)(c.work + c.L.ring);
+    float *ring2 = (float *)(c.work + c.L.ring2);
+    float *ck = (float *)(c.work + c.L.ckpt);
+    const size_t fbytes = sizeof(float) * g.fstride;
+    const size_t ring_pitch = 3 * fbytes, ck_pitch = 2 * (size_t)nseg * fbytes;
+    long long launches = 0;
+    auto profile_span = [&](cudaEvent_t &e0, cudaEvent_t &e1) {
+        e0 = e1 = nullptr;
+        if (c.profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
+            cudaEventRecord(e0, st);
+    };
+    auto close_span = [&](cudaEvent_t e0, cudaEvent_t e1, long long n) {
+        if (!e1) return;
+        cudaEventRecord(e1, st);
+        t_profile.spans.emplace_back(e0, e1);
+        t_profile.launches += n;
+    };
+    cudaEvent_t e0, e1;
+
+    // forward: data only, checkpoints at segment starts
+    b.ring = ring;
+    b.store = 0;
+    cudaMemset2DAsync(ring, ring_pitch, 0, 2 * fbytes, nres, st);
+    profile_span(e0, e1);
+    for (int k = 0; k < g.nt; ++k) {
+        if (k % K == 0) {
+            const int s = k / K;
+            cudaMemcpy2DAsync((char *)ck + (size_t)2 * s * fbytes, ck_pitch, (char *)ring + (size_t)(k % 3) * fbytes,
+                              ring_pitch, fbytes, nres, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpy2DAsync((char *)ck + (size_t)(2 * s + 1) * fbytes, ck_pitch,
+                              (char *)ring + (size_t)((k + 1) % 3) * fbytes, ring_pitch, fbytes, nres,
+                              cudaMemcpyDeviceToDevice, st);
+        }
+        StepArgs sa;
+        sa.k = k;
+        sa.it = k;
+        sa.snap = -1;
+        sa.rik = c.d->rik[k];
+        step(false, c.maps, g, b, nres, sa, st);
+        ++launches;
+    }
+    close_span(e0, e1, g.nt);
+
+    // adjoint, segment by segment from the last
+    cudaMemset2DAsync(ring2, ring_pitch, 0, 2 * fbytes, nres, st);
+    Batch ba = b;
+    ba.ring = ring2;
+    b.store = 1;
+    profile_span(e0, e1);
+    for (int s = nseg - 1; s >= 0; --s) {
+        const int k0 = s * K, k1 = std::min(k0 + K, g.nt), snap0 = k0 / g.nti;
+        cudaMemcpy2DAsync((char *)ring + (size_t)(k0 % 3) * fbytes, ring_pitch, (char *)ck + (size_t)2 * s * fbytes,
+                          ck_pitch, fbytes, nres, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpy2DAsync((char *)ring + (size_t)((k0 + 1) % 3) * fbytes, ring_pitch,
+                          (char *)ck + (size_t)(2 * s + 1) * fbytes, ck_pitch, fbytes, nres,
+                          cudaMemcpyDeviceToDevice, st);
+        for (int k = k0; k < k1; ++k) {  // recompute the segment's forward steps, storing them
+            StepArgs sa;
+            sa.k = k;
+            sa.it = k;
+            sa.snap = (k % g.nti) == 0 ? k / g.nti - snap0 : -1;
+            sa.rik = c.d->rik[k];
+            step(false, c.maps, g, b, nres, sa, st);
+            ++launches;
+        }
+        for (int it = k1 - 1; it >= k0; --it) {  // the segment's adjoint steps
+            StepArgs sa;
+            sa.k = g.nt - 1 - it;
+            sa.it = it;
+            sa.snap = (it % g.nti) == 0 ? it / g.nti - snap0 : -1;
+            sa.rik = 0.0f;
+            step(true, c.maps2, g, ba, nres, sa, st);
+            ++launches;
+        }
+    }
+    close_span(e0, e1, 2LL * g.nt);
+    return launches;
 }
 
 // Enqueue the whole batch on `st`; returns the number of kernel launches.
@@ -511,7 +625,13 @@ static long long enqueue(const Call &c, cudaStream_t st)
     const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
-    for (long long i0 = 0; i0 < ninst; i0 += wave) {
+    const bool ckpt = (c.flags & GB_FWI2D_CHECKPOINT) && !fwd_only;
+    for (long long i0 = 0; i0 < ninst && ckpt; i0 += wave) {
+        const int nres = (int)std::min<long long>(wave, ninst - i0);
+        b.inst0 = (int)i0;
+        launches += enqueue_checkpointed(c, b, nres, st);
+    }
+    for (long long i0 = 0; i0 < ninst && !ckpt; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
         b.inst0 = (int)i0;
         for (int pass = 0; pass < (fwd_only ? 1 : 2); ++pass) {
@@ -671,7 +791,9 @@ size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_
     if (!p || nsamples <= 0) return 0;
     Derived d;
     if (derive(*p, d)) return 0;
-    return plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0).total;
+    return plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0,
+                       (flags & GB_FWI2D_CHECKPOINT) != 0)
+        .total;
 }
 
 int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
@@ -680,11 +802,11 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
 {
     t_last_launches = 0;
     if (!p || nsamples <= 0 || !vel || !obs || !work) return GB_FWI2D_EINVAL;
-    if (flags & GB_FWI2D_CHECKPOINT) return GB_FWI2D_ENOTSUP;
     Derived d;
     int st = derive(*p, d);
     if (st) return st;
-    Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0);
+    const bool ckpt = (flags & GB_FWI2D_CHECKPOINT) != 0;
+    Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0, ckpt);
     if (work_bytes < L.total) return GB_FWI2D_ENOMEM;
     Call c;
     c.d = &d;
@@ -699,6 +821,9 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     c.work = (char *)work;
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
     if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
+        return GB_FWI2D_ECUDA;
+    if (ckpt && !(flags & GB_FWI2D_FORWARD_ONLY) &&
+        !make_maps(c.maps2, d.g, (float *)(c.work + L.ring2), L.resident))
         return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);
     if (st) return st;

@@ -43,10 +43,13 @@ class Fwi2dEngine:
         None sizes it from ``hbm_budget`` (bytes, default 60% of free memory).
     graph: capture the step sequence in a CUDA graph on first use and replay.
     plain: one solve per launch, shots in order -- the comparator form.
+    checkpoint: keep the forward state every ~sqrt(nt) steps and recompute
+        each segment in the adjoint (for solves whose stored field would not fit).
     """
 
     def __init__(self, params: Params, device=None, max_resident: int | None = None,
-                 hbm_budget: int | None = None, graph: bool = True, plain: bool = False):
+                 hbm_budget: int | None = None, graph: bool = True, plain: bool = False,
+                 checkpoint: bool = False):
         self.params = params
         self.lib = _native.load()
         self.device = torch.device(device if device is not None else "cuda")
@@ -59,6 +62,7 @@ class Fwi2dEngine:
         self.hbm_budget = hbm_budget
         self.graph = graph
         self.plain = plain
+        self.checkpoint = checkpoint
         self._cp = params.c()
         self._work: torch.Tensor | None = None
         self._work_key = None
@@ -131,6 +135,8 @@ class Fwi2dEngine:
             flags |= _native.FLAG_IMAGING
         if self.plain:
             flags |= _native.FLAG_PLAIN
+        if self.checkpoint:
+            flags |= _native.FLAG_CHECKPOINT
         if profile:
             flags |= _native.FLAG_PROFILE
         elif self.graph and not self.plain:

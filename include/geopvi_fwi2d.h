@@ -54,7 +54,9 @@ typedef struct gb_fwi2d_params {
 #define GB_FWI2D_IMAGING 0x1u    /* run_fwi = 0: zero-lag imaging (record = obs, psave = p) */
 #define GB_FWI2D_PLAIN 0x2u      /* one (sample, shot) per launch, shots in order (comparator) */
 #define GB_FWI2D_GRAPH 0x4u      /* capture the step sequence once in a CUDA graph, replay after */
-#define GB_FWI2D_CHECKPOINT 0x8u /* store sqrt(nt) checkpoints, recompute the forward in segments */
+#define GB_FWI2D_CHECKPOINT 0x8u /* keep (p0,p1) every ~sqrt(nt) steps, recompute the forward per
+                                    segment in the adjoint: 1.5x the steps, ~sqrt(nt)/nt_save the
+                                    stored-field memory; results identical to full storage */
 #define GB_FWI2D_FORWARD_ONLY 0x10u /* synthetic data only (forward_2D): no adjoint, no stored field */
 #define GB_FWI2D_PROFILE 0x20u   /* time the step-kernel loops with CUDA events (not with GRAPH) */
 

@@ -131,3 +131,13 @@ def test_batch_rejects_bad_arguments_without_gpu(engine_lib):
     bad = p.replace(laplace_solver=1).c()
     st = engine_lib.gb_fwi2d_batch(ctypes.byref(bad), 1, 1, 1, None, None, None, 0, 0, 1, 1 << 30, None)
     assert st == _native.ENOTSUP
+
+
+def test_checkpoint_workspace_is_smaller(engine_lib):
+    from geopvi_gb300 import workloads
+    p = workloads.cfg3().params
+    cp = p.c()
+    full = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 32, 0)
+    ck = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 32, _native.FLAG_CHECKPOINT)
+    # 32 solves of 300x600, nt 4000: full storage ~93 GB, checkpoints ~5 GB
+    assert ck * 10 < full

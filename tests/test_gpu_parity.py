@@ -164,3 +164,18 @@ def test_status_word_clear_after_runs(engine_lib, cuda):
     st = engine_lib.gb_fwi2d_status(ctypes.c_void_p(eng._work.data_ptr()),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert st == 0
+
+
+@pytest.mark.parametrize("name", ["fwi_o8", "fwi_o8_nti2", "fwi_o10_nti3", "img_o6"])
+def test_checkpointing_is_bit_identical_to_full_storage(engine_lib, cuda, name):
+    """sqrt(nt) checkpoints with segment recomputation reproduce full storage exactly."""
+    z = load(name)
+    p = cases.params_from_npz(z)
+    imaging = int(z["run_fwi"]) == 0
+    vels = np.stack([z["start"], z["truth"], z["start"] * np.float32(0.99)])
+    ref = run(engine_for(p, graph=False), vels, z["obs"], imaging=imaging, want_syn=True)
+    for kw in (dict(checkpoint=True), dict(checkpoint=True, max_resident=2), dict(checkpoint=True, graph=True)):
+        o = run(engine_for(p, **kw), vels, z["obs"], imaging=imaging, want_syn=True)
+        assert np.array_equal(o["syn"], ref["syn"]), kw
+        assert np.array_equal(o["grad"], ref["grad"]), kw
+        assert np.array_equal(o["misfit"], ref["misfit"]), kw
