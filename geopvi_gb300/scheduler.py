@@ -1,0 +1,321 @@
+"""Continuous batching of misfit + gradient requests on one GPU.
+
+GeoPVI evaluates its likelihood one VI iteration at a time, one sample after
+another (geopvi/forward/fwi2d/posterior.py:112-149).  This module serves many
+such evaluations at once: requests from several inversions (each with its own
+grid, acquisition, time axis and observed data) arrive at any time; a
+dispatcher thread admits them as HBM and streams free up, merges queued
+requests of the same inversion into one batch, chooses how each batch holds
+its forward field (full storage in waves, or sqrt(nt) checkpoints) from a
+cost model, and runs admitted batches concurrently on a pool of CUDA streams.
+Observed data stay resident per inversion; each request's workspace lives
+only while it runs.
+
+Every kernel is deterministic and a solve never reads another solve's memory,
+so a request's result does not depend on what ran beside it (the tests check
+this bit for bit).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import queue
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native
+from .params import Params
+
+# Cost model of one step launch on GB300, fitted to measured launches of the
+# step kernel (profile_step, bench plain mode): t = LAUNCH_OVERHEAD_S +
+# padded cells / CELL_RATE (one cfg2 solve, 0.11 M cells: 29 us; 140 solves,
+# 15.8 M cells: 195 us; 1280 solves, 144 M cells: 1.44 ms).
+CELL_RATE = 1.0e11
+LAUNCH_OVERHEAD_S = 25e-6
+
+
+@dataclass
+class Plan:
+    """How one batch runs: resident solves per wave, storage mode, bytes, cost."""
+    resident: int
+    checkpoint: bool
+    nbytes: int
+    est_seconds: float
+
+
+def _ws(lib, cp, nsamples, resident, flags):
+    return int(lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), nsamples, resident, flags))
+
+
+def plan_batch(p: Params, nsamples: int, cap_bytes: int, lib=None) -> Plan | None:
+    """Cheapest (storage mode, wave size) whose workspace fits in cap_bytes.
+
+    Full storage runs 2*nt steps per wave; checkpointing 3*nt but needs
+    ~sqrt(nt)/nt_save of the stored field, so more solves fit per wave.  A
+    step launch costs LAUNCH_OVERHEAD_S + cells / CELL_RATE."""
+    lib = lib or _native.load()
+    cp = p.c()
+    ninst = nsamples * p.ns
+    best = None
+    for ckpt in (False, True):
+        flags = _native.FLAG_CHECKPOINT if ckpt else 0
+        base = _ws(lib, cp, nsamples, 1, flags)
+        if base == 0 or base > cap_bytes:
+            continue
+        per = _ws(lib, cp, nsamples, 2, flags) - base if ninst > 1 else 0
+        r = ninst if per <= 0 else int(min(ninst, 1 + (cap_bytes - base) // per))
+        waves = math.ceil(ninst / r)
+        steps = (3 if ckpt else 2) * p.nt
+        t_launch = LAUNCH_OVERHEAD_S + r * p.ntp / CELL_RATE
+        est = waves * steps * t_launch
+        cand = Plan(resident=r, checkpoint=ckpt, nbytes=_ws(lib, cp, nsamples, r, flags), est_seconds=est)
+        if best is None or cand.est_seconds < best.est_seconds:
+            best = cand
+    return best
+
+
+@dataclass
+class Request:
+    inversion: str
+    vel: torch.Tensor                  # (n, nz*nx) float32, host or device
+    want_syn: bool = False
+    future: Future = field(default_factory=Future)
+    t_submit: float = 0.0
+    t_start: float = 0.0
+    t_done: float = 0.0
+
+    @property
+    def nsamples(self) -> int:
+        return int(self.vel.shape[0])
+
+
+@dataclass
+class _Inversion:
+    params: Params
+    obs: torch.Tensor                  # device-resident observed data
+    imaging: bool
+
+
+@dataclass
+class _Running:
+    requests: list
+    stream: torch.cuda.Stream
+    event: torch.cuda.Event
+    work: torch.Tensor
+    vel: torch.Tensor
+    misfit: torch.Tensor
+    grad: torch.Tensor
+    syn: torch.Tensor | None
+    plan: Plan
+    inversion: _Inversion
+
+
+class FwiServer:
+    """Dispatcher for misfit + gradient requests.
+
+    hbm_budget: bytes of device memory the running batches' workspaces may hold
+        together (observed data and outputs are counted separately).
+    streams: batches that may run at once.
+    max_group_samples: queued requests of one inversion merged up to this many
+        samples per batch.
+    Results are host tensors: misfit float64 (n,), gradient float32 (n, nz*nx)
+    in the reference's scaling (the array fwi_2D accumulates), and the
+    synthetic data (n, ns*nt*nr) when asked.
+    """
+
+    def __init__(self, device=None, hbm_budget: int = 150 << 30, streams: int = 4, max_group_samples: int = 64):
+        self.device = torch.device(device if device is not None else "cuda")
+        self.lib = _native.load()
+        self.budget = int(hbm_budget)
+        self.max_group_samples = max_group_samples
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(streams)]
+        self._free_streams = list(self._streams)
+        self._inv: dict[str, _Inversion] = {}
+        self._queue: "queue.Queue[Request]" = queue.Queue()
+        self._pending: list[Request] = []
+        self._running: list[_Running] = []
+        self._used = 0
+        self._stop = threading.Event()
+        self._thread: threading.Thread | None = None
+        self.completed: list[Request] = []
+        self.busy_seconds = 0.0
+
+    # ---- inversions ----
+    def register(self, name: str, params: Params, obs, imaging: bool = False) -> None:
+        """Upload an inversion's observed data (ns*nt*nr float32); it stays resident."""
+        params.validate()
+        obs = torch.as_tensor(np.ascontiguousarray(obs, dtype=np.float32) if not isinstance(obs, torch.Tensor) else obs)
+        obs = obs.to(self.device, torch.float32).reshape(-1).contiguous()
+        torch.cuda.synchronize(self.device)  # the batches read it from their own streams
+        if obs.numel() != params.data_len:
+            raise ValueError(f"observed data has {obs.numel()} values, expected {params.data_len}")
+        self._inv[name] = _Inversion(params, obs, imaging)
+
+    # ---- requests ----
+    def submit(self, name: str, vel, want_syn: bool = False) -> Future:
+        if name not in self._inv:
+            raise KeyError(f"unknown inversion {name!r}")
+        vel = vel if isinstance(vel, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(vel, dtype=np.float32))
+        if vel.dim() == 1:
+            vel = vel.unsqueeze(0)
+        if vel.shape[1] != self._inv[name].params.ncell:
+            raise ValueError("velocity models do not match the inversion's grid")
+        if torch.isnan(vel).any():
+            raise ValueError("NaN occured in sample!")
+        r = Request(name, vel.to(torch.float32), want_syn)
+        r.t_submit = time.perf_counter()
+        self._queue.put(r)
+        return r.future
+
+    def start(self) -> "FwiServer":
+        self._stop.clear()
+        self._thread = threading.Thread(target=self._loop, name="fwi-dispatch", daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self) -> None:
+        self._stop.set()
+        if self._thread:
+            self._thread.join()
+            self._thread = None
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    def drain(self, timeout: float | None = None) -> None:
+        """Wait until every submitted request finished."""
+        t0 = time.perf_counter()
+        while True:
+            if self._queue.empty() and not self._pending and not self._running:
+                return
+            if timeout is not None and time.perf_counter() - t0 > timeout:
+                raise TimeoutError("requests still running")
+            time.sleep(0.002)
+
+    # ---- dispatcher ----
+    def _loop(self) -> None:
+        torch.cuda.set_device(self.device)
+        while not self._stop.is_set():
+            progressed = self._reap()
+            while True:
+                try:
+                    self._pending.append(self._queue.get_nowait())
+                except queue.Empty:
+                    break
+            progressed |= self._admit()
+            if not progressed:
+                time.sleep(0.0005)
+        # finish what runs, fail what never started
+        while self._running:
+            self._reap()
+            time.sleep(0.001)
+        for r in self._pending:
+            r.future.set_exception(RuntimeError("server stopped before the request ran"))
+        self._pending.clear()
+
+    def _reap(self) -> bool:
+        done = [g for g in self._running if g.event.query()]
+        for g in done:
+            self._running.remove(g)
+            try:
+                g.stream.synchronize()
+                misfit = g.misfit.cpu()
+                grad = g.grad.cpu()
+                syn = g.syn.cpu() if g.syn is not None else None
+                st = int(self.lib.gb_fwi2d_status(ctypes.c_void_p(g.work.data_ptr()), ctypes.c_void_p(g.stream.cuda_stream)))
+                now = time.perf_counter()
+                i = 0
+                for r in g.requests:
+                    n = r.nsamples
+                    r.t_done = now
+                    if st != _native.OK:
+                        r.future.set_exception(_native.EngineError(st, "device status"))
+                    else:
+                        res = {"misfit": misfit[i:i + n], "grad": grad[i:i + n]}
+                        if r.want_syn and syn is not None:
+                            res["syn"] = syn[i:i + n]
+                        r.future.set_result(res)
+                    self.completed.append(r)
+                    i += n
+            except Exception as e:  # pragma: no cover - device errors surface here
+                for r in g.requests:
+                    if not r.future.done():
+                        r.future.set_exception(e)
+            finally:
+                self._used -= g.plan.nbytes
+                self._free_streams.append(g.stream)
+        return bool(done)
+
+    def _admit(self) -> bool:
+        admitted = False
+        while self._pending and self._free_streams:
+            head = self._pending[0]
+            inv = self._inv[head.inversion]
+            group, n = [], 0
+            for r in list(self._pending):
+                if r.inversion == head.inversion and n + r.nsamples <= max(self.max_group_samples, head.nsamples):
+                    group.append(r)
+                    n += r.nsamples
+            free = self.budget - self._used
+            # a batch may take all of the free budget when it runs alone, half otherwise
+            cap = free if not self._running else free // 2
+            plan = plan_batch(inv.params, n, cap, self.lib)
+            if plan is None:
+                if not self._running:
+                    for r in group:
+                        self._pending.remove(r)
+                        r.future.set_exception(_native.EngineError(_native.ENOMEM, "request exceeds the HBM budget"))
+                    continue
+                break  # wait for memory to free up
+            for r in group:
+                self._pending.remove(r)
+            self._launch(group, inv, plan)
+            admitted = True
+        return admitted
+
+    def _launch(self, group: list, inv: _Inversion, plan: Plan) -> None:
+        stream = self._free_streams.pop()
+        p = inv.params
+        n = sum(r.nsamples for r in group)
+        want_syn = any(r.want_syn for r in group)
+        now = time.perf_counter()
+        for r in group:
+            r.t_start = now
+        with torch.cuda.stream(stream):
+            work = torch.empty(plan.nbytes, dtype=torch.uint8, device=self.device)
+            vel = torch.cat([r.vel.to(self.device, non_blocking=True) for r in group]).contiguous()
+            misfit = torch.empty(n, dtype=torch.float64, device=self.device)
+            grad = torch.empty(n, p.ncell, dtype=torch.float32, device=self.device)
+            syn = torch.empty(n, p.data_len, dtype=torch.float32, device=self.device) if want_syn else None
+            flags = (_native.FLAG_IMAGING if inv.imaging else 0) | (_native.FLAG_CHECKPOINT if plan.checkpoint else 0)
+            cp = p.c()
+            st = self.lib.gb_fwi2d_batch(ctypes.byref(cp), n, vel.data_ptr(), inv.obs.data_ptr(),
+                                         syn.data_ptr() if syn is not None else None, grad.data_ptr(),
+                                         misfit.data_ptr(), flags, plan.resident, work.data_ptr(), plan.nbytes,
+                                         ctypes.c_void_p(stream.cuda_stream))
+            event = torch.cuda.Event()
+            event.record(stream)
+        if st != _native.OK:
+            self._free_streams.append(stream)
+            for r in group:
+                r.future.set_exception(_native.EngineError(st, "gb_fwi2d_batch"))
+            return
+        self._used += plan.nbytes
+        self._running.append(_Running(group, stream, event, work, vel, misfit, grad, syn, plan, inv))
+
+
+def latency_summary(requests: list) -> dict:
+    """p50 / p99 / max latency (seconds) from submit to result."""
+    lat = np.array([r.t_done - r.t_submit for r in requests if r.t_done > 0])
+    if lat.size == 0:
+        return {"count": 0}
+    return {"count": int(lat.size), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "max_s": float(lat.max()), "mean_s": float(lat.mean())}

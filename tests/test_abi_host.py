@@ -141,3 +141,15 @@ def test_checkpoint_workspace_is_smaller(engine_lib):
     ck = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 32, _native.FLAG_CHECKPOINT)
     # 32 solves of 300x600, nt 4000: full storage ~93 GB, checkpoints ~5 GB
     assert ck * 10 < full
+
+
+def test_batch_plan_prefers_checkpoints_when_memory_is_tight(engine_lib):
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import plan_batch
+    p = workloads.cfg3().params  # 300x600, nt 4000, 32 shots: ~2.9 GB stored field per solve
+    roomy = plan_batch(p, 16, 4 << 40)
+    assert roomy is not None and not roomy.checkpoint and roomy.resident == 16 * 32
+    # 8 GB holds one full-storage solve beside the synthetic data, ~19 checkpointed ones
+    tight = plan_batch(p, 16, 8 << 30)
+    assert tight is not None and tight.checkpoint and tight.nbytes <= 8 << 30 and tight.resident > 10
+    assert plan_batch(p, 16, 1 << 20) is None
