@@ -47,7 +47,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"],
+                    help="cfg4: uneven batch of 48 instances; cfg5: serving loop (own JSON line)")
+    ap.add_argument("--requests", type=int, default=12, help="cfg5: requests served")
+    ap.add_argument("--rate", type=float, default=200.0, help="cfg5: mean Poisson arrival rate (req/s)")
     ap.add_argument("--cpu-shots", type=int, default=2, help="shots in the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -59,6 +62,8 @@ def parse_args():
 
 def workload(name: str, nt: int | None = None):
     from geopvi_gb300 import workloads
+    if name not in ("cfg1", "cfg2", "cfg3"):
+        name = "cfg2"  # the reference arm times the batched VI iteration's per-shot cost
     w = {"cfg1": workloads.cfg1, "cfg2": workloads.cfg2, "cfg3": workloads.cfg3}[name]()
     if nt:
         w.params = w.params.replace(nt=nt)
@@ -203,7 +208,7 @@ def run_reference(args):
         "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD_NAMES[args.config], "sample": desc},
+        "config": {"workload": WORKLOAD_NAMES.get(args.config, WORKLOAD_NAMES["cfg2"]), "sample": desc},
         "sample_gradients_per_s": value / cell_updates_per_sample(p),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": kind, "sample": desc},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -385,12 +390,136 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# cfg4 (uneven batch) and cfg5 (serving): whole-job runs through the scheduler
+# ---------------------------------------------------------------------------
+def _observed(p, truth, dev):
+    import torch
+    from geopvi_gb300.engine import Fwi2dEngine
+    eng = Fwi2dEngine(p, device=dev, graph=False, checkpoint=True)
+    zeros = torch.zeros(p.data_len, dtype=torch.float32, device=dev)
+    obs = eng.run(torch.from_numpy(truth).to(dev).unsqueeze(0), zeros, forward_only=True).syn[0].cpu()
+    del eng
+    return obs
+
+
+def _instance_models(p, rng, nsamples):
+    from geopvi_gb300 import workloads
+    truth = workloads.gradient_with_anomalies(p.nz, p.nx, p.dx, rng)
+    base = workloads.smooth(truth)
+    samples = np.stack([base + rng.uniform(-150.0, 150.0, base.shape) for _ in range(nsamples)])
+    return truth.astype(np.float32).ravel(), samples.reshape(nsamples, -1).astype(np.float32)
+
+
+def run_uneven(args):
+    """cfg4: 48 instances of mixed grid, shots, nt and f0 submitted at once."""
+    import torch
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import FwiServer
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    plist = workloads.cfg4_instances()
+    rng = np.random.default_rng(40)
+    jobs = []
+    for i, p in enumerate(plist):
+        truth, samples = _instance_models(p, rng, 1)
+        jobs.append((f"inst{i}", p, samples, _observed(p, truth, dev)))
+    cells = sum(cell_updates_per_sample(p) for _, p, _, _ in jobs)
+    with FwiServer(device=dev, streams=4) as srv:
+        for name, p, _, obs in jobs:
+            srv.register(name, p, obs)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        futs = [srv.submit(name, vel) for name, _, vel, _ in jobs]
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": cells / wall,
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded models)",
+        "config": {"workload": "uneven batch: 48 instances, grids {100x200..400x800}, 4-48 shots, "
+                               "nt 1500-5000, Ricker 5-12 Hz, 1 model each, submitted at once",
+                   "instances": len(jobs), "cell_updates": cells,
+                   "storage": "per batch: full storage in waves or sqrt(nt) checkpoints (cost model)"},
+        "sample_gradients_per_s": len(jobs) / wall,
+        "e2e": {"value": cells / wall, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(sum(v.nbytes for _, _, v, _ in jobs)),
+                "d2h_bytes_per_step": int(sum(8 + 4 * p.ncell for _, p, _, _ in jobs)),
+                "api": "geopvi_gb300.scheduler.FwiServer (host models in, host results out)"},
+    }), flush=True)
+
+
+def run_serving(args):
+    """cfg5: Poisson arrivals of misfit+gradient requests from 6 inversions."""
+    import torch
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import FwiServer, latency_summary
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(50)
+    grids = [(120, 250), (200, 400), (300, 600), (400, 800)]
+    kinds = ["advi", "advi", "flow", "flow", "bvi", "bvi"]      # mean-field ADVI, flows, boosting VI
+    batch = {"advi": (4, 8), "flow": (16, 32), "bvi": (8, 16)}  # samples per request
+    inv = []
+    for i, kind in enumerate(kinds):
+        nz, nx = grids[rng.integers(len(grids))]
+        p = workloads.make_params(nz, nx, int(rng.integers(2000, 5001)), 1e-3, int(rng.integers(10, 41)),
+                                  round(float(rng.uniform(6.0, 12.0)), 2))
+        truth, _ = _instance_models(p, rng, 1)
+        inv.append((f"{kind}{i}", kind, p, truth, _observed(p, truth, dev)))
+    reqs = []
+    for _ in range(args.requests):
+        name, kind, p, truth, _ = inv[rng.integers(len(inv))]
+        lo, hi = batch[kind]
+        n = int(rng.integers(lo, hi + 1))
+        base = workloads.smooth(truth.reshape(p.nz, p.nx))
+        vel = (base[None] + rng.normal(0.0, 60.0, (n,) + base.shape)).reshape(n, -1).astype(np.float32)
+        reqs.append((name, p, vel))
+    gaps = rng.exponential(1.0 / args.rate, len(reqs))
+    with FwiServer(device=dev, streams=4) as srv:
+        for name, _, p, _, obs in inv:
+            srv.register(name, p, obs)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        futs = []
+        for (name, p, vel), gap in zip(reqs, gaps):
+            time.sleep(gap)
+            futs.append(srv.submit(name, vel))
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t0
+        lat = latency_summary(srv.completed)
+    cells = sum(cell_updates_per_sample(p) * vel.shape[0] for _, p, vel in reqs)
+    grads = sum(vel.shape[0] for _, _, vel in reqs)
+    print(json.dumps({
+        "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": cells / wall,
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded models)",
+        "config": {"workload": f"serving: {len(reqs)} requests, Poisson arrivals at {args.rate} req/s, "
+                               "6 inversions (2 ADVI, 2 flow, 2 BVI), 4-32 samples, grids 120x250..400x800, "
+                               "10-40 shots, nt 2000-5000, 150 GB admission budget",
+                   "requests": len(reqs), "samples": grads},
+        "sample_gradients_per_s": grads / wall, "latency": lat,
+        "e2e": {"value": cells / wall, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(sum(v.nbytes for _, _, v in reqs)),
+                "d2h_bytes_per_step": int(sum(v.shape[0] * (8 + 4 * p.ncell) for _, p, v in reqs)),
+                "api": "geopvi_gb300.scheduler.FwiServer"},
+    }), flush=True)
+
+
 def main():
     args = parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "cfg4":
+        run_uneven(args)
+    elif args.config == "cfg5":
+        run_serving(args)
     else:
         run_gpu(args)
 
