@@ -421,9 +421,12 @@ def run_uneven(args):
     plist = workloads.cfg4_instances()
     rng = np.random.default_rng(40)
     jobs = []
+    t_setup = time.perf_counter()
     for i, p in enumerate(plist):
         truth, samples = _instance_models(p, rng, 1)
         jobs.append((f"inst{i}", p, samples, _observed(p, truth, dev)))
+    print(f"cfg4: observed data for {len(jobs)} instances in {time.perf_counter() - t_setup:.1f} s",
+          file=sys.stderr, flush=True)
     cells = sum(cell_updates_per_sample(p) for _, p, _, _ in jobs)
     with FwiServer(device=dev, streams=4) as srv:
         for name, p, _, obs in jobs:
@@ -431,8 +434,9 @@ def run_uneven(args):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         futs = [srv.submit(name, vel) for name, _, vel, _ in jobs]
-        for f in futs:
+        for k, f in enumerate(futs):
             f.result()
+            print(f"cfg4: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
     print(json.dumps({
         "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": cells / wall,
@@ -487,8 +491,9 @@ def run_serving(args):
         for (name, p, vel), gap in zip(reqs, gaps):
             time.sleep(gap)
             futs.append(srv.submit(name, vel))
-        for f in futs:
+        for k, f in enumerate(futs):
             f.result()
+            print(f"cfg5: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
         lat = latency_summary(srv.completed)
     cells = sum(cell_updates_per_sample(p) * vel.shape[0] for _, p, vel in reqs)
