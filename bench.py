@@ -396,10 +396,11 @@ def run_gpu(args):
 def _observed(p, truth, dev):
     import torch
     from geopvi_gb300.engine import Fwi2dEngine
-    eng = Fwi2dEngine(p, device=dev, graph=False, checkpoint=True)
+    eng = Fwi2dEngine(p, device=dev, graph=False, hbm_budget=8 << 30)
     zeros = torch.zeros(p.data_len, dtype=torch.float32, device=dev)
     obs = eng.run(torch.from_numpy(truth).to(dev).unsqueeze(0), zeros, forward_only=True).syn[0].cpu()
-    del eng
+    del eng, zeros
+    torch.cuda.empty_cache()
     return obs
 
 
@@ -435,7 +436,7 @@ def run_uneven(args):
         t0 = time.perf_counter()
         futs = [srv.submit(name, vel) for name, _, vel, _ in jobs]
         for k, f in enumerate(futs):
-            f.result()
+            f.result(timeout=600)
             print(f"cfg4: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
     print(json.dumps({
@@ -492,7 +493,7 @@ def run_serving(args):
             time.sleep(gap)
             futs.append(srv.submit(name, vel))
         for k, f in enumerate(futs):
-            f.result()
+            f.result(timeout=600)
             print(f"cfg5: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
         lat = latency_summary(srv.completed)

@@ -79,6 +79,46 @@ def plan_batch(p: Params, nsamples: int, cap_bytes: int, lib=None) -> Plan | Non
     return best
 
 
+class Arena:
+    """First-fit sub-allocator over one device buffer (256-byte granules).
+
+    The server's workspaces come from here instead of the framework's caching
+    allocator, so admission can reason about one contiguous budget and
+    requests of changing sizes do not fragment device memory."""
+
+    ALIGN = 256
+
+    def __init__(self, nbytes: int):
+        self.size = nbytes // self.ALIGN * self.ALIGN
+        self.free = [(0, self.size)]  # sorted (offset, length)
+
+    def largest(self) -> int:
+        return max((n for _, n in self.free), default=0)
+
+    def alloc(self, nbytes: int) -> int | None:
+        need = (nbytes + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+        for i, (off, n) in enumerate(self.free):
+            if n >= need:
+                if n == need:
+                    self.free.pop(i)
+                else:
+                    self.free[i] = (off + need, n - need)
+                return off
+        return None
+
+    def release(self, off: int, nbytes: int) -> None:
+        need = (nbytes + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+        self.free.append((off, need))
+        self.free.sort()
+        merged = []
+        for o, n in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == o:
+                merged[-1] = (merged[-1][0], merged[-1][1] + n)
+            else:
+                merged.append((o, n))
+        self.free = merged
+
+
 @dataclass
 class Request:
     inversion: str
@@ -106,7 +146,8 @@ class _Running:
     requests: list
     stream: torch.cuda.Stream
     event: torch.cuda.Event
-    work: torch.Tensor
+    work_off: int
+    work_ptr: int
     vel: torch.Tensor
     misfit: torch.Tensor
     grad: torch.Tensor
@@ -118,8 +159,9 @@ class _Running:
 class FwiServer:
     """Dispatcher for misfit + gradient requests.
 
-    hbm_budget: bytes of device memory the running batches' workspaces may hold
-        together (observed data and outputs are counted separately).
+    hbm_budget: bytes of the one device arena the running batches' workspaces
+        are carved from (allocated when the server starts; observed data and
+        outputs are separate, small allocations).
     streams: batches that may run at once.
     max_group_samples: queued requests of one inversion merged up to this many
         samples per batch.
@@ -139,7 +181,8 @@ class FwiServer:
         self._queue: "queue.Queue[Request]" = queue.Queue()
         self._pending: list[Request] = []
         self._running: list[_Running] = []
-        self._used = 0
+        self._arena: Arena | None = None
+        self._arena_mem: torch.Tensor | None = None
         self._stop = threading.Event()
         self._thread: threading.Thread | None = None
         self.completed: list[Request] = []
@@ -173,6 +216,10 @@ class FwiServer:
         return r.future
 
     def start(self) -> "FwiServer":
+        if self._arena_mem is None:
+            torch.cuda.empty_cache()
+            self._arena_mem = torch.empty(self.budget, dtype=torch.uint8, device=self.device)
+            self._arena = Arena(self.budget)
         self._stop.clear()
         self._thread = threading.Thread(target=self._loop, name="fwi-dispatch", daemon=True)
         self._thread.start()
@@ -183,6 +230,8 @@ class FwiServer:
         if self._thread:
             self._thread.join()
             self._thread = None
+        self._arena_mem = None
+        self._arena = None
 
     def __enter__(self):
         return self.start()
@@ -204,13 +253,20 @@ class FwiServer:
     def _loop(self) -> None:
         torch.cuda.set_device(self.device)
         while not self._stop.is_set():
-            progressed = self._reap()
-            while True:
-                try:
-                    self._pending.append(self._queue.get_nowait())
-                except queue.Empty:
-                    break
-            progressed |= self._admit()
+            try:
+                progressed = self._reap()
+                while True:
+                    try:
+                        self._pending.append(self._queue.get_nowait())
+                    except queue.Empty:
+                        break
+                progressed |= self._admit()
+            except Exception as e:  # a failure fails the requests it touched, never the loop
+                for r in self._pending:
+                    if not r.future.done():
+                        r.future.set_exception(e)
+                self._pending.clear()
+                progressed = False
             if not progressed:
                 time.sleep(0.0005)
         # finish what runs, fail what never started
@@ -230,7 +286,7 @@ class FwiServer:
                 misfit = g.misfit.cpu()
                 grad = g.grad.cpu()
                 syn = g.syn.cpu() if g.syn is not None else None
-                st = int(self.lib.gb_fwi2d_status(ctypes.c_void_p(g.work.data_ptr()), ctypes.c_void_p(g.stream.cuda_stream)))
+                st = int(self.lib.gb_fwi2d_status(ctypes.c_void_p(g.work_ptr), ctypes.c_void_p(g.stream.cuda_stream)))
                 now = time.perf_counter()
                 i = 0
                 for r in g.requests:
@@ -250,7 +306,7 @@ class FwiServer:
                     if not r.future.done():
                         r.future.set_exception(e)
             finally:
-                self._used -= g.plan.nbytes
+                self._arena.release(g.work_off, g.plan.nbytes)
                 self._free_streams.append(g.stream)
         return bool(done)
 
@@ -264,8 +320,8 @@ class FwiServer:
                 if r.inversion == head.inversion and n + r.nsamples <= max(self.max_group_samples, head.nsamples):
                     group.append(r)
                     n += r.nsamples
-            free = self.budget - self._used
-            # a batch may take all of the free budget when it runs alone, half otherwise
+            free = self._arena.largest()
+            # a batch may take all of the free arena when it runs alone, half otherwise
             cap = free if not self._running else free // 2
             plan = plan_batch(inv.params, n, cap, self.lib)
             if plan is None:
@@ -277,11 +333,20 @@ class FwiServer:
                 break  # wait for memory to free up
             for r in group:
                 self._pending.remove(r)
-            self._launch(group, inv, plan)
+            try:
+                self._launch(group, inv, plan)
+            except Exception as e:
+                for r in group:
+                    if not r.future.done():
+                        r.future.set_exception(e)
             admitted = True
         return admitted
 
     def _launch(self, group: list, inv: _Inversion, plan: Plan) -> None:
+        off = self._arena.alloc(plan.nbytes)
+        if off is None:
+            raise _native.EngineError(_native.ENOMEM, "arena")
+        work_ptr = self._arena_mem.data_ptr() + off
         stream = self._free_streams.pop()
         p = inv.params
         n = sum(r.nsamples for r in group)
@@ -290,7 +355,6 @@ class FwiServer:
         for r in group:
             r.t_start = now
         with torch.cuda.stream(stream):
-            work = torch.empty(plan.nbytes, dtype=torch.uint8, device=self.device)
             vel = torch.cat([r.vel.to(self.device, non_blocking=True) for r in group]).contiguous()
             misfit = torch.empty(n, dtype=torch.float64, device=self.device)
             grad = torch.empty(n, p.ncell, dtype=torch.float32, device=self.device)
@@ -299,17 +363,17 @@ class FwiServer:
             cp = p.c()
             st = self.lib.gb_fwi2d_batch(ctypes.byref(cp), n, vel.data_ptr(), inv.obs.data_ptr(),
                                          syn.data_ptr() if syn is not None else None, grad.data_ptr(),
-                                         misfit.data_ptr(), flags, plan.resident, work.data_ptr(), plan.nbytes,
+                                         misfit.data_ptr(), flags, plan.resident, work_ptr, plan.nbytes,
                                          ctypes.c_void_p(stream.cuda_stream))
             event = torch.cuda.Event()
             event.record(stream)
         if st != _native.OK:
             self._free_streams.append(stream)
+            self._arena.release(off, plan.nbytes)
             for r in group:
                 r.future.set_exception(_native.EngineError(st, "gb_fwi2d_batch"))
             return
-        self._used += plan.nbytes
-        self._running.append(_Running(group, stream, event, work, vel, misfit, grad, syn, plan, inv))
+        self._running.append(_Running(group, stream, event, off, work_ptr, vel, misfit, grad, syn, plan, inv))
 
 
 def latency_summary(requests: list) -> dict:

@@ -153,3 +153,19 @@ def test_batch_plan_prefers_checkpoints_when_memory_is_tight(engine_lib):
     tight = plan_batch(p, 16, 8 << 30)
     assert tight is not None and tight.checkpoint and tight.nbytes <= 8 << 30 and tight.resident > 10
     assert plan_batch(p, 16, 1 << 20) is None
+
+
+def test_arena_first_fit_and_merge():
+    from geopvi_gb300.scheduler import Arena
+    a = Arena(10 * 256)
+    x = a.alloc(300)   # 2 granules
+    y = a.alloc(256)
+    z = a.alloc(1000)  # 4 granules
+    assert (x, y, z) == (0, 512, 768) and a.largest() == 3 * 256
+    assert a.alloc(4 * 256) is None
+    a.release(y, 256)
+    a.release(x, 300)
+    assert a.largest() == 3 * 256 and a.alloc(3 * 256) == 0
+    a.release(0, 3 * 256)
+    a.release(z, 1000)
+    assert a.free == [(0, 10 * 256)]
