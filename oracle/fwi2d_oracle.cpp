@@ -35,6 +35,7 @@
  *   - loops run row-major (iz outer, ix inner) with OpenMP over rows;
  *   - errors are returned as negative status codes instead of exit().
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -381,6 +382,183 @@ int run_forward_impl(const oracle_params *pp, const Real *vel_inner, Real *recor
     return ORACLE_OK;
 }
 
+
+/* ------------------------------------------------------------------------
+ * Exact discrete adjoint (double precision).
+ *
+ * One step of the scheme maps the two previous levels to the next one
+ * linearly: p2 = A1 p1 + A0 p0 + f_it, where for each cell c
+ *   p2_c = beta_c * S_c + sum_b gamma_{c,b} * E_{c,b}
+ * with S_c the stencil value 2 p1 - p0 + a_c (Dxx + Dzz) p1 (a_c = (v dt)^2)
+ * inside the stencil region and the copied p1_c outside it, E_{c,b} the
+ * one-way extrapolation of blend b (top/bottom, then left/right) with
+ * weights w_b: beta = prod (1 - w_b), gamma_1 = w_1 (1 - w_2), gamma_2 = w_2.
+ * With lambda^k = dJ/dP^k for J = 1/2 sum_t |R P^{t+1} - obs_t|^2:
+ *   lambda^k = R^T r_{k-1} + A1^T lambda^{k+1} + A0^T lambda^{k+2},
+ *   dJ/dv_c  = sum_t lambda^{t+1}_c d(p2_c)/d(v_c) |_{step t},
+ * and the padded-grid derivative is summed back onto the interior cells the
+ * padding replicates (get_velp is a clamp).  This is the gradient a central
+ * finite difference of the scheme converges to; the reference's own
+ * gradient (backward_IO) is a continuous-adjoint approximation of it.
+ * ------------------------------------------------------------------------ */
+struct CellOp {
+    bool sten;
+    double beta;
+    int nb;
+    int step[2];
+    double gam[2];
+};
+
+static void cell_ops(const Geometry &g, const std::vector<double> &w, std::vector<CellOp> &ops)
+{
+    const int ntx = g.ntx, ntz = g.ntz, Lc = g.Lc, pml = g.pml;
+    ops.assign((size_t)g.ntp, CellOp{});
+    for (int iz = 0; iz < ntz; ++iz)
+        for (int ix = 0; ix < ntx; ++ix) {
+            CellOp &o = ops[(size_t)iz * ntx + ix];
+            o.sten = iz >= Lc && iz < ntz - Lc && ix >= Lc && ix < ntx - Lc;
+            double wv[2];
+            o.nb = 0;
+            if (iz >= Lc && iz < pml) { o.step[o.nb] = ntx; wv[o.nb++] = w[iz - Lc]; }
+            else if (iz >= ntz - pml && iz < ntz - Lc) { o.step[o.nb] = -ntx; wv[o.nb++] = w[ntz - Lc - iz - 1]; }
+            if (ix >= Lc && ix < pml) { o.step[o.nb] = 1; wv[o.nb++] = w[ix - Lc]; }
+            else if (ix >= ntx - pml && ix < ntx - Lc) { o.step[o.nb] = -1; wv[o.nb++] = w[ntx - Lc - ix - 1]; }
+            if (o.nb == 0) o.beta = 1.0;
+            else if (o.nb == 1) { o.beta = 1.0 - wv[0]; o.gam[0] = wv[0]; }
+            else { o.beta = (1.0 - wv[0]) * (1.0 - wv[1]); o.gam[0] = wv[0] * (1.0 - wv[1]); o.gam[1] = wv[1]; }
+        }
+}
+
+struct ExactShot {
+    const oracle_params &p;
+    const Geometry &g;
+    Engine<double> &e;
+    std::vector<CellOp> ops;
+
+    ExactShot(const oracle_params &pp, const Geometry &gg, Engine<double> &ee) : p(pp), g(gg), e(ee)
+    {
+        std::vector<double> w(e.w.begin(), e.w.end());
+        cell_ops(g, w, ops);
+    }
+
+    // out += A1^T lam (p1 coefficients) or A0^T lam (p0 coefficients).
+    void scatter(const double *lam, double *out, bool p1op) const
+    {
+        const int ntx = g.ntx;
+        const int H = g.Lc - 1;
+        const double rdx2 = 1.0 / ((double)e.dx * e.dx), rdz2 = 1.0 / ((double)e.dz * e.dz);
+        for (int c = 0; c < g.ntp; ++c) {
+            const double l = lam[c];
+            if (l == 0.0) continue;
+            const CellOp &o = ops[c];
+            const double bl = o.beta * l;
+            if (o.sten) {
+                if (p1op) {
+                    const double a = e.vdt2[c];
+                    out[c] += 2.0 * bl + bl * a * e.fd[0] * (rdx2 + rdz2);
+                    for (int m = 1; m <= H; ++m) {
+                        const double kx = bl * a * e.fd[m] * rdx2, kz = bl * a * e.fd[m] * rdz2;
+                        out[c + m] += kx;
+                        out[c - m] += kx;
+                        out[c + m * ntx] += kz;
+                        out[c - m * ntx] += kz;
+                    }
+                } else {
+                    out[c] -= bl;
+                }
+            } else if (p1op) {
+                out[c] += bl;  // the copied previous level
+            }
+            for (int b = 0; b < o.nb; ++b) {
+                const double gl = o.gam[b] * l;
+                const int st = o.step[b];
+                const double t11 = e.t11[c], t12 = e.t12[c], t13 = e.t13[c];
+                if (p1op) {
+                    out[c] += gl * 2 * t11;
+                    out[c + st] += gl * 2 * t12;
+                    out[c + 2 * st] += gl * 2 * t13;
+                } else {
+                    out[c] -= gl * t11 * t11;
+                    out[c + st] -= gl * 2 * t11 * t12;
+                    out[c + 2 * st] -= gl * (t12 * t12 + 2 * t11 * t13);
+                    out[c + 3 * st] -= gl * 2 * t12 * t13;
+                    out[c + 4 * st] -= gl * t13 * t13;
+                }
+            }
+        }
+    }
+
+    // d(p2_c)/d(v_c) at one step, from the step's p1, p0 and source value.
+    double dp2_dv(int c, const double *p1, const double *p0, double rik_it, int src) const
+    {
+        const CellOp &o = ops[c];
+        const int ntx = g.ntx, H = g.Lc - 1;
+        const double v = e.velp[c], dt = e.dt, dx = e.dx, dz = e.dz;
+        double d = 0.0;
+        if (o.sten) {
+            double lx = e.fd[0] * p1[c], lz = e.fd[0] * p1[c];
+            for (int m = 1; m <= H; ++m) {
+                lx += e.fd[m] * (p1[c + m] + p1[c - m]);
+                lz += e.fd[m] * (p1[c + m * ntx] + p1[c - m * ntx]);
+            }
+            d += o.beta * 2.0 * v * dt * dt * (lx / (dx * dx) + lz / (dz * dz));
+        }
+        if (o.nb) {
+            const double s = v * dt / dx;
+            const double t11 = (2 - s) * (1 - s) / 2, t12 = s * (2 - s), t13 = s * (s - 1) / 2;
+            const double u11 = (2 * s - 3) / 2, u12 = 2 - 2 * s, u13 = (2 * s - 1) / 2;  // d t / d s
+            for (int b = 0; b < o.nb; ++b) {
+                const int st = o.step[b];
+                const double dE = 2 * u11 * p1[c] + 2 * u12 * p1[c + st] + 2 * u13 * p1[c + 2 * st] -
+                                  2 * t11 * u11 * p0[c] - 2 * (u11 * t12 + t11 * u12) * p0[c + st] -
+                                  (2 * t12 * u12 + 2 * u11 * t13 + 2 * t11 * u13) * p0[c + 2 * st] -
+                                  2 * (u12 * t13 + t12 * u13) * p0[c + 3 * st] - 2 * t13 * u13 * p0[c + 4 * st];
+                d += o.gam[b] * dE * dt / dx;
+            }
+        }
+        if (c == src) d += 2.0 * rik_it * dt * dt * v;
+        return d;
+    }
+
+    // Misfit of the shot and its exact gradient on the padded grid (added to gpad).
+    double run(int is, const double *obs, double *gpad)
+    {
+        const int ntp = g.ntp, nt = p.nt, nr = p.nr;
+        const int src = g.s_iz * g.ntx + g.s_ix[is];
+        std::vector<double> P((size_t)(nt + 2) * ntp, 0.0);  // level k at (k + 1) * ntp, k = -1..nt
+        auto lev = [&](int k) { return P.data() + (size_t)(k + 1) * ntp; };
+        std::vector<double> resid((size_t)nt * nr);
+        e.zero_fields();
+        double J = 0.0;
+        for (int it = 0; it < nt; ++it) {
+            e.stencil();
+            e.boundary();
+            e.p2[src] += e.rik[it] * e.dt * e.dt * e.velp[src] * e.velp[src];
+            std::copy(e.p2.begin(), e.p2.end(), lev(it + 1));
+            for (int ir = 0; ir < nr; ++ir) {
+                const double r = e.p2[g.r_iz * g.ntx + g.r_ix[ir]] - obs[(size_t)it * nr + ir];
+                resid[(size_t)it * nr + ir] = r;
+                J += 0.5 * r * r;
+            }
+            e.rotate();
+        }
+        std::vector<double> l0(ntp, 0.0), l1(ntp, 0.0), l2(ntp, 0.0);  // lambda^k, ^k+1, ^k+2
+        for (int k = nt; k >= 1; --k) {
+            std::fill(l0.begin(), l0.end(), 0.0);
+            for (int ir = 0; ir < nr; ++ir) l0[g.r_iz * g.ntx + g.r_ix[ir]] += resid[(size_t)(k - 1) * nr + ir];
+            scatter(l1.data(), l0.data(), true);
+            scatter(l2.data(), l0.data(), false);
+            const int it = k - 1;  // the step whose p2 is level k
+            const double *p1 = lev(it), *p0 = lev(it - 1);
+            for (int c = 0; c < ntp; ++c)
+                if (l0[c] != 0.0) gpad[c] += l0[c] * dp2_dv(c, p1, p0, e.rik[it], src);
+            std::swap(l2, l1);
+            std::swap(l1, l0);
+        }
+        return J;
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -420,6 +598,32 @@ int oracle_forward2d_f32(const oracle_params *p, const float *vel, float *syn)
 int oracle_forward2d_f64(const oracle_params *p, const double *vel, double *syn)
 {
     return run_forward_impl<double>(p, vel, syn);
+}
+
+/* Exact discrete gradient dJ/dv of J = 1/2 sum (syn - obs)^2 over all shots,
+ * in double precision (see ExactShot); returns J. */
+int oracle_exact_grad_f64(const oracle_params *pp, const double *vel, const double *obs, double *grad,
+                          double *misfit)
+{
+    Geometry g;
+    int st = make_geometry(*pp, g);
+    if (st) return st;
+    Engine<double> e(*pp, g);
+    e.pad_velocity(vel);
+    ExactShot x(*pp, g, e);
+    std::vector<double> gpad((size_t)g.ntp, 0.0);
+    double J = 0.0;
+    const size_t shot_len = (size_t)pp->nt * pp->nr;
+    for (int is = 0; is < pp->ns; ++is) J += x.run(is, obs + is * shot_len, gpad.data());
+    for (int i = 0; i < pp->nz * pp->nx; ++i) grad[i] = 0.0;
+    for (int iz = 0; iz < g.ntz; ++iz)
+        for (int ix = 0; ix < g.ntx; ++ix) {
+            const int jz = std::min(std::max(iz - g.pml, 0), pp->nz - 1);
+            const int jx = std::min(std::max(ix - g.pml, 0), pp->nx - 1);
+            grad[jz * pp->nx + jx] += gpad[(size_t)iz * g.ntx + ix];
+        }
+    if (misfit) *misfit = J;
+    return ORACLE_OK;
 }
 
 /* Ricker table as the float solver sees it (getrik, fdtd2D_modelling.c:1084). */

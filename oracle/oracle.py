@@ -126,6 +126,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_fwi2d_f64.argtypes = [P, fp64, fp64, fp64, fp64, ctypes.c_int]
         L.oracle_forward2d_f32.argtypes = [P, fp32, fp32]
         L.oracle_forward2d_f64.argtypes = [P, fp64, fp64]
+        L.oracle_exact_grad_f64.argtypes = [P, fp64, fp64, fp64, fp64]
         L.oracle_read_params.argtypes = [ctypes.c_char_p, P]
         L.oracle_ricker_f32.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float, fp32]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
@@ -211,6 +212,26 @@ def forward_f64(p: Params, vel):
     if st:
         raise ValueError(f"oracle_forward2d_f64 status {st}")
     return syn
+
+
+def exact_grad_f64(p: Params, vel, obs):
+    """(misfit, dJ/dv f64[nz*nx]): the exact gradient of the discrete scheme
+    (double precision) for J = 0.5 * sum((syn - obs)^2) over all shots."""
+    vel = np.ascontiguousarray(vel, dtype=np.float64).ravel()
+    obs = np.ascontiguousarray(obs, dtype=np.float64).ravel()
+    grad = np.zeros(p.nz * p.nx, np.float64)
+    J = ctypes.c_double(0.0)
+    cp = p.c()
+    st = lib().oracle_exact_grad_f64(ctypes.byref(cp), _ptr(vel, ctypes.c_double), _ptr(obs, ctypes.c_double),
+                                     _ptr(grad, ctypes.c_double), ctypes.byref(J))
+    if st:
+        raise ValueError(f"oracle_exact_grad_f64 status {st}")
+    return J.value, grad
+
+
+def misfit_f64(p: Params, vel, obs) -> float:
+    syn = forward_f64(p, vel)
+    return float(0.5 * np.sum((syn - np.asarray(obs, np.float64).ravel()) ** 2))
 
 
 def ricker_f32(nt: int, dt: float, f0: float) -> np.ndarray:
