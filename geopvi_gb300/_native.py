@@ -32,6 +32,7 @@ FLAG_GRAPH = 0x4
 FLAG_CHECKPOINT = 0x8
 FLAG_FORWARD_ONLY = 0x10
 FLAG_PROFILE = 0x20
+FLAG_EXACT_GRADIENT = 0x40
 
 STATIC_SCRATCH_BYTES = 64 << 20
 

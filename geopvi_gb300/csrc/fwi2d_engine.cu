@@ -23,6 +23,7 @@
 
 #include "../../include/geopvi_fwi2d.h"
 #include "fwi2d_kernels.cuh"
+#include "fwi2d_exact_adjoint.cuh"
 
 namespace gbfwi {
 
@@ -212,6 +213,7 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
 struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
     size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
+    size_t store, lam, gpad;  // exact gradient only: forward levels, adjoint levels, padded dJ/dv
     int resident;
     int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
 };
@@ -230,12 +232,41 @@ constexpr int kMisfitBlocks = 64;  // partial sums per sample for the misfit
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Exact gradient: the adjoint needs every forward level, kept either for all
+// nt steps (one segment) or, with checkpointing, for one ceil(sqrt(nt))-step
+// segment at a time: store holds the segment's K+1 levels P^{i0-1} .. P^{i0+K-1}.
+static Layout plan_layout_exact(const Geom &g, int nsamples, int resident, bool syn_in_work, bool checkpoint)
+{
+    Layout L{};
+    const long long ninst = (long long)nsamples * g.ns;
+    L.resident = resident;
+    L.ckpt_k = checkpoint ? std::max(1, (int)std::ceil(std::sqrt((double)g.nt))) : g.nt;
+    L.ckpt_nseg = (g.nt + L.ckpt_k - 1) / L.ckpt_k;
+    const size_t field = sizeof(float) * g.fstride;
+    size_t off = 0;
+    L.status = off; off = align256(off + sizeof(int));
+    L.vdt = off;    off = align256(off + field * nsamples);
+    L.ring = off;   off = align256(off + field * 3 * resident);
+    L.ckpt = off;
+    if (L.ckpt_nseg > 1) off = align256(off + field * 2 * L.ckpt_nseg * resident);
+    L.store = off;  off = align256(off + field * (L.ckpt_k + 1) * resident);
+    L.lam = off;    off = align256(off + field * 3 * resident);
+    L.gpad = off;   off = align256(off + field * ninst);
+    L.psave = L.gacc = off;
+    L.syn = off;
+    if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
+    L.part = off;   off = align256(off + sizeof(double) * kMisfitBlocks * nsamples);
+    L.total = off;
+    return L;
+}
+
 static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in_work,
-                          bool forward_only, bool checkpoint = false)
+                          bool forward_only, bool checkpoint = false, bool exact = false)
 {
     Layout L{};
     const long long ninst = (long long)nsamples * g.ns;
     if (resident <= 0 || resident > ninst) resident = (int)ninst;
+    if (exact && !forward_only) return plan_layout_exact(g, nsamples, resident, syn_in_work, checkpoint);
     L.resident = resident;
     checkpoint = checkpoint && !forward_only;
     long long snaps = g.nt_save;  // stored steps per resident solve
@@ -587,9 +618,145 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
     return launches;
 }
 
+template <int H>
+static void launch_adjoint_exact(const Geom &g, const ExactBatch &x, int nres, int k, int lev1, float rik,
+                                 cudaStream_t st)
+{
+    const dim3 grid((unsigned)((g.fstride + 255) / 256), nres);
+    k_adjoint_exact<H><<<grid, 256, 0, st>>>(g, x, k, lev1, rik);
+}
+
+static void adjoint_exact(const Geom &g, const ExactBatch &x, int nres, int k, int lev1, float rik, cudaStream_t st)
+{
+    switch (g.Lc - 1) {
+    case 3: launch_adjoint_exact<3>(g, x, nres, k, lev1, rik, st); break;
+    case 4: launch_adjoint_exact<4>(g, x, nres, k, lev1, rik, st); break;
+    case 5: launch_adjoint_exact<5>(g, x, nres, k, lev1, rik, st); break;
+    default: launch_adjoint_exact<6>(g, x, nres, k, lev1, rik, st); break;
+    }
+}
+
+// Exact gradient.  Per wave: the forward pass (data, and either every level
+// into `store` or a (p0, p1) pair per segment), then the segments from the
+// last: restore the pair, recompute the segment's levels into `store`, and
+// run its adjoint steps k = i1 .. i0+1, each of which needs lambda^{k+1},
+// lambda^{k+2} and the levels P^{k-1}, P^{k-2}.  Levels come out of the
+// forward ring with one strided device copy per step.
+static long long enqueue_exact(const Call &c, cudaStream_t st)
+{
+    const Geom &g = c.d->g;
+    const Layout &L = c.L;
+    long long launches = 0;
+    float *vdt = (float *)(c.work + L.vdt);
+    float *ring = (float *)(c.work + L.ring);
+    float *ck = (float *)(c.work + L.ckpt);
+    float *store = (float *)(c.work + L.store);
+    float *lam = (float *)(c.work + L.lam);
+    float *gpad = (float *)(c.work + L.gpad);
+    float *syn = c.syn ? c.syn : (float *)(c.work + L.syn);
+    double *part = (double *)(c.work + L.part);
+    int *status = (int *)(c.work + L.status);
+    const long long ninst = (long long)c.nsamples * g.ns;
+    const int K = L.ckpt_k, nseg = L.ckpt_nseg;
+    const size_t fbytes = sizeof(float) * g.fstride;
+    const size_t ring_pitch = 3 * fbytes, store_pitch = (size_t)(K + 1) * fbytes, ck_pitch = 2 * (size_t)nseg * fbytes;
+
+    k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt, c.nsamples);
+    ++launches;
+    cudaMemsetAsync(status, 0, sizeof(int), st);
+    cudaMemsetAsync(gpad, 0, fbytes * ninst, st);
+
+    Batch b{};
+    b.vdt = vdt;
+    b.vel = c.vel;
+    b.obs = c.obs;
+    b.syn = syn;
+    b.ring = ring;
+    b.coef = c.tab.coef;
+    b.blend_fp32 = c.d->blend_fp32 ? 1 : 0;
+    b.status = status;
+    ExactBatch x;
+    x.vdt = vdt;
+    x.obs = c.obs;
+    x.syn = syn;
+    x.lam = lam;
+    x.store = store;
+    x.store_pitch = (long long)(K + 1) * g.fstride;
+    x.gpad = gpad;
+    x.coef = c.tab.coef;
+
+    auto fwd = [&](int it, int nres) {
+        StepArgs sa;
+        sa.k = it;
+        sa.it = it;
+        sa.snap = -1;
+        sa.rik = c.d->rik[it];
+        step(false, c.maps, g, b, nres, sa, st);
+        ++launches;
+    };
+    auto level_out = [&](int it, int slot_level, int nres) {  // P^{it+1} -> store level
+        cudaMemcpy2DAsync((char *)store + (size_t)slot_level * fbytes, store_pitch,
+                          (char *)ring + (size_t)((it + 2) % 3) * fbytes, ring_pitch, fbytes, nres,
+                          cudaMemcpyDeviceToDevice, st);
+    };
+    const int wave = (c.flags & GB_FWI2D_PLAIN) ? 1 : L.resident;
+    for (long long i0 = 0; i0 < ninst; i0 += wave) {
+        const int nres = (int)std::min<long long>(wave, ninst - i0);
+        b.inst0 = x.inst0 = (int)i0;
+        cudaMemset2DAsync(ring, ring_pitch, 0, 2 * fbytes, nres, st);
+        if (nseg == 1) cudaMemset2DAsync(store, store_pitch, 0, 2 * fbytes, nres, st);  // P^-1 = P^0 = 0
+        for (int it = 0; it < g.nt; ++it) {
+            if (nseg > 1 && it % K == 0) {
+                const int s = it / K;  // the step's (p0, p1) = (P^{it-1}, P^it)
+                for (int h = 0; h < 2; ++h)
+                    cudaMemcpy2DAsync((char *)ck + (size_t)(2 * s + h) * fbytes, ck_pitch,
+                                      (char *)ring + (size_t)((it + h) % 3) * fbytes, ring_pitch, fbytes, nres,
+                                      cudaMemcpyDeviceToDevice, st);
+            }
+            fwd(it, nres);
+            if (nseg == 1 && it <= g.nt - 2) level_out(it, it + 2, nres);
+        }
+        cudaMemsetAsync(lam, 0, 3 * fbytes * (size_t)nres, st);
+        for (int s = nseg - 1; s >= 0; --s) {
+            const int i0s = s * K, i1s = std::min(i0s + K, g.nt);
+            if (nseg > 1) {
+                // the pair (P^{i0s-1}, P^{i0s}) into the ring's p0, p1 and store levels 0, 1
+                for (int h = 0; h < 2; ++h) {
+                    const char *src = (char *)ck + (size_t)(2 * s + h) * fbytes;
+                    cudaMemcpy2DAsync((char *)ring + (size_t)((i0s + h) % 3) * fbytes, ring_pitch, src, ck_pitch,
+                                      fbytes, nres, cudaMemcpyDeviceToDevice, st);
+                    cudaMemcpy2DAsync((char *)store + (size_t)h * fbytes, store_pitch, src, ck_pitch, fbytes, nres,
+                                      cudaMemcpyDeviceToDevice, st);
+                }
+                for (int it = i0s; it <= i1s - 2; ++it) {
+                    fwd(it, nres);
+                    level_out(it, it - i0s + 2, nres);
+                }
+            }
+            for (int k = i1s; k >= i0s + 1; --k) {
+                adjoint_exact(g, x, nres, k, k - i0s, c.d->rik[k - 1], st);
+                ++launches;
+            }
+        }
+    }
+    if (c.grad) {
+        k_reduce_exact<<<grid_for((long long)c.nsamples * g.nz * g.nx, 256), 256, 0, st>>>(g, gpad, c.grad,
+                                                                                           c.nsamples);
+        ++launches;
+    }
+    if (c.misfit) {
+        k_misfit_partial<<<dim3(kMisfitBlocks, c.nsamples), 256, 0, st>>>(syn, c.obs, (long long)g.ns * g.nt * g.nr,
+                                                                          part);
+        k_misfit_final<<<(c.nsamples + 127) / 128, 128, 0, st>>>(part, c.misfit, c.nsamples);
+        launches += 2;
+    }
+    return launches;
+}
+
 // Enqueue the whole batch on `st`; returns the number of kernel launches.
 static long long enqueue(const Call &c, cudaStream_t st)
 {
+    if ((c.flags & GB_FWI2D_EXACT_GRADIENT) && !(c.flags & GB_FWI2D_FORWARD_ONLY)) return enqueue_exact(c, st);
     const Geom &g = c.d->g;
     long long launches = 0;
     float *vdt = (float *)(c.work + c.L.vdt);
@@ -792,7 +959,7 @@ size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_
     Derived d;
     if (derive(*p, d)) return 0;
     return plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0,
-                       (flags & GB_FWI2D_CHECKPOINT) != 0)
+                       (flags & GB_FWI2D_CHECKPOINT) != 0, (flags & GB_FWI2D_EXACT_GRADIENT) != 0)
         .total;
 }
 
@@ -806,7 +973,9 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     int st = derive(*p, d);
     if (st) return st;
     const bool ckpt = (flags & GB_FWI2D_CHECKPOINT) != 0;
-    Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0, ckpt);
+    const bool exact = (flags & GB_FWI2D_EXACT_GRADIENT) != 0;
+    if (exact && (flags & GB_FWI2D_IMAGING)) return GB_FWI2D_EINVAL;
+    Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0, ckpt, exact);
     if (work_bytes < L.total) return GB_FWI2D_ENOMEM;
     Call c;
     c.d = &d;
@@ -822,7 +991,7 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
     if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
         return GB_FWI2D_ECUDA;
-    if (ckpt && !(flags & GB_FWI2D_FORWARD_ONLY) &&
+    if (ckpt && !exact && !(flags & GB_FWI2D_FORWARD_ONLY) &&
         !make_maps(c.maps2, d.g, (float *)(c.work + L.ring2), L.resident))
         return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);

@@ -1,0 +1,234 @@
+// fwi2d_exact_adjoint.cuh -- exact discrete adjoint of the FD scheme.
+//
+// The reference's gradient (backward_IO, geopvi/forward/fwi2d/
+// fdtd2D_modelling.c:941-978) back-propagates the residual with the forward
+// operator and correlates it with the stored second time derivative: a
+// continuous-adjoint approximation, about dt * dJ/dv and a few degrees off
+// in direction.  Finite-difference checks of dJ/dv need the transpose of the
+// scheme itself.  One step maps the two previous levels linearly,
+//   p2_c = beta_c * S_c + sum_b gamma_{c,b} * E_{c,b} (+ source),
+// S_c the stencil value 2 p1 - p0 + a_c (Dxx + Dzz) p1 inside the stencil
+// region (a_c = (v dt)^2) and the copied p1_c outside it, E_{c,b} the
+// one-way extrapolation of boundary blend b (top/bottom first, then
+// left/right) with weight w_b: beta = prod (1 - w_b), gamma_1 = w_1 (1 - w_2),
+// gamma_2 = w_2.  With lambda^k = dJ/dP^k for J = 1/2 sum |R P^{t+1} - obs_t|^2,
+//   lambda^k = R^T r_{k-1} + A1^T lambda^{k+1} + A0^T lambda^{k+2},
+//   dJ/dv_c += lambda^{t+1}_c * d p2_c / d v_c  (step t: p1 = P^t, p0 = P^{t-1}).
+// k_adjoint_exact computes lambda^k for every cell as a gather over the
+// cells whose update reads it, and accumulates the padded-grid gradient;
+// k_reduce_exact sums it back onto the interior cells that get_velp's
+// padding replicates.  FP32 arithmetic: this path has no reference output to
+// match bit for bit; the FP64 oracle of the same recursion is its check.
+#pragma once
+
+#include "fwi2d_kernels.cuh"
+
+namespace gbfwi {
+
+struct ExactBatch {
+    const float *vdt;      // [nsamples][fstride] padded v*dt
+    const float *obs;      // [ns][nt][nr]
+    const float *syn;      // [nsamples*ns][nt][nr]
+    float *lam;            // [resident][3][fstride] adjoint levels
+    const float *store;    // [resident][levels][fstride] forward levels of the segment
+    long long store_pitch; // floats between resident slots of `store`
+    float *gpad;           // [nsamples*ns][fstride] padded-grid dJ/dv
+    const BlendCoef *coef; // boundary weights
+    int inst0;
+};
+
+// Blend facts of one padded cell: blends applied in order (top/bottom, then
+// left/right), their inward steps and weights, beta and gamma.
+struct CellInfo {
+    bool sten;   // in the stencil region
+    int nb;      // blends 0..2
+    int dir[2];  // 0 top (+z inward), 1 bottom (-z), 2 left (+x), 3 right (-x)
+    float beta, gam[2];
+};
+
+__device__ __forceinline__ CellInfo cell_info(const Geom &g, const BlendCoef *coef, int iz, int ix)
+{
+    CellInfo ci;
+    ci.sten = iz >= g.Lc && iz < g.ntz - g.Lc && ix >= g.Lc && ix < g.ntx - g.Lc;
+    float w[2] = {0.0f, 0.0f};
+    ci.nb = 0;
+    ci.dir[0] = ci.dir[1] = -1;
+    if (iz >= g.Lc && iz < g.pml) { ci.dir[ci.nb] = 0; w[ci.nb++] = coef[iz - g.Lc].w; }
+    else if (iz >= g.ntz - g.pml && iz < g.ntz - g.Lc) { ci.dir[ci.nb] = 1; w[ci.nb++] = coef[g.ntz - g.Lc - iz - 1].w; }
+    if (ix >= g.Lc && ix < g.pml) { ci.dir[ci.nb] = 2; w[ci.nb++] = coef[ix - g.Lc].w; }
+    else if (ix >= g.ntx - g.pml && ix < g.ntx - g.Lc) { ci.dir[ci.nb] = 3; w[ci.nb++] = coef[g.ntx - g.Lc - ix - 1].w; }
+    ci.beta = 1.0f;
+    ci.gam[0] = ci.gam[1] = 0.0f;
+    if (ci.nb == 1) {
+        ci.beta = 1.0f - w[0];
+        ci.gam[0] = w[0];
+    } else if (ci.nb == 2) {
+        ci.beta = (1.0f - w[0]) * (1.0f - w[1]);
+        ci.gam[0] = w[0] * (1.0f - w[1]);
+        ci.gam[1] = w[1];
+    }
+    return ci;
+}
+
+// beta_c of a stencil-region cell, 0 elsewhere (and off the grid).
+__device__ __forceinline__ float stencil_beta(const Geom &g, const BlendCoef *coef, int iz, int ix)
+{
+    if (iz < g.Lc || iz >= g.ntz - g.Lc || ix < g.Lc || ix >= g.ntx - g.Lc) return 0.0f;
+    float beta = 1.0f;
+    if (iz < g.pml) beta = 1.0f - coef[iz - g.Lc].w;
+    else if (iz >= g.ntz - g.pml) beta = 1.0f - coef[g.ntz - g.Lc - iz - 1].w;
+    if (ix < g.pml) beta *= 1.0f - coef[ix - g.Lc].w;
+    else if (ix >= g.ntx - g.pml) beta *= 1.0f - coef[g.ntx - g.Lc - ix - 1].w;
+    return beta;
+}
+
+// Extrapolation weights of s = v dt / dx (abc_for_p's t11, t12, t13).
+struct Taps {
+    float t11, t12, t13;
+};
+__device__ __forceinline__ Taps taps_of(float s)
+{
+    return Taps{(2.0f - s) * (1.0f - s) * 0.5f, s * (2.0f - s), s * (s - 1.0f) * 0.5f};
+}
+
+// Step k of the backward recursion for every cell of every resident solve:
+// lambda^k into lam[k % 3], and dJ/dv_j += lambda^k_j * d p2_j / d v_j of
+// forward step k-1, whose inputs P^{k-1} and P^{k-2} sit in store levels
+// `lev1` and lev1 - 1.  rik_prev = the Ricker value of step k-1.
+template <int H>
+__global__ void __launch_bounds__(256)
+    k_adjoint_exact(const Geom g, const ExactBatch b, int k, int lev1, float rik_prev)
+{
+    const int slot = blockIdx.y;
+    const int inst = b.inst0 + slot;
+    const int sample = inst / g.ns, shot = inst - sample * g.ns;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= g.fstride) return;
+    const int iz = (int)(e / g.pitch);
+    const int ix = (int)(e - (long long)iz * g.pitch) - g.xoff;
+    if (ix < 0 || ix >= g.ntx) return;
+    const long long P = g.pitch;
+    const long long j = e;
+
+    const float *vdt = b.vdt + (long long)sample * g.fstride;
+    float *l_base = b.lam + (long long)slot * 3 * g.fstride;
+    const float *lam1 = l_base + (long long)((k + 1) % 3) * g.fstride;  // lambda^{k+1}
+    const float *lam2 = l_base + (long long)((k + 2) % 3) * g.fstride;  // lambda^{k+2}
+    float *lam0 = l_base + (long long)(k % 3) * g.fstride;
+    const float rdx2 = 1.0f / (g.dx * g.dx), rdz2 = 1.0f / (g.dz * g.dz);
+
+    float out = 0.0f;
+    // R^T r_{k-1}: the residual of step k-1 at a receiver cell
+    if (iz == g.r_iz) {
+        const int ir = receiver_of(g, ix);
+        if (ir >= 0) {
+            const long long t = (long long)(k - 1) * g.nr + ir;
+            out += b.syn[(long long)inst * g.nt * g.nr + t] - b.obs[(long long)shot * g.nt * g.nr + t];
+        }
+    }
+    const CellInfo cj = cell_info(g, b.coef, iz, ix);
+    // A1^T lambda^{k+1}: nu_c = a_c beta_c lambda_c over the stencil cells c reading j
+    auto nu = [&](int cz, int cx) -> float {
+        const float beta = stencil_beta(g, b.coef, cz, cx);
+        if (beta == 0.0f) return 0.0f;
+        const long long c = (long long)cz * P + cx + g.xoff;
+        const float vd = vdt[c];
+        return vd * vd * beta * lam1[c];
+    };
+    if (cj.sten) {
+        out += 2.0f * cj.beta * lam1[j] + fd_weight<H>(0) * (rdx2 + rdz2) * nu(iz, ix);
+        out -= cj.beta * lam2[j];  // A0^T lambda^{k+2}
+    } else {
+        out += cj.beta * lam1[j];  // the copied level
+    }
+#pragma unroll
+    for (int m = 1; m <= H; ++m)
+        out += fd_weight<H>(m) * (rdx2 * (nu(iz, ix + m) + nu(iz, ix - m)) + rdz2 * (nu(iz + m, ix) + nu(iz - m, ix)));
+    // Blend taps: cell c = j - kk * step_d (kk <= 4) in blend band d reads p1
+    // at kk <= 2 and p0 at kk <= 4 steps inward of itself.
+    const bool near_band = iz < g.pml + 4 || iz >= g.ntz - g.pml - 4 || ix < g.pml + 4 || ix >= g.ntx - g.pml - 4;
+    if (near_band) {
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            const int sz = d == 0 ? 1 : d == 1 ? -1 : 0, sx = d == 2 ? 1 : d == 3 ? -1 : 0;
+#pragma unroll
+            for (int kk = 0; kk <= 4; ++kk) {
+                const int cz = iz - kk * sz, cx = ix - kk * sx;
+                if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) continue;
+                const CellInfo c = cell_info(g, b.coef, cz, cx);
+                const float gam = c.dir[0] == d ? c.gam[0] : c.dir[1] == d ? c.gam[1] : 0.0f;
+                if (gam == 0.0f) continue;
+                const long long ci = (long long)cz * P + cx + g.xoff;
+                const Taps t = taps_of(vdt[ci] / g.dx);
+                const float c1 = kk == 0 ? 2.0f * t.t11 : kk == 1 ? 2.0f * t.t12 : kk == 2 ? 2.0f * t.t13 : 0.0f;
+                const float c0 = kk == 0   ? t.t11 * t.t11
+                                 : kk == 1 ? 2.0f * t.t11 * t.t12
+                                 : kk == 2 ? t.t12 * t.t12 + 2.0f * t.t11 * t.t13
+                                 : kk == 3 ? 2.0f * t.t12 * t.t13
+                                           : t.t13 * t.t13;
+                out += gam * (c1 * lam1[ci] - c0 * lam2[ci]);
+            }
+        }
+    }
+    lam0[j] = out;
+    if (out == 0.0f) return;
+
+    // d p2_j / d v_j of step k-1
+    const float *st = b.store + (long long)slot * b.store_pitch;
+    const float *p1 = st + (long long)lev1 * g.fstride;
+    const float *p0 = p1 - g.fstride;
+    const float v = vdt[j] / g.dt;
+    float d = 0.0f;
+    if (cj.sten) {
+        float lx = fd_weight<H>(0) * p1[j], lz = lx;
+#pragma unroll
+        for (int m = 1; m <= H; ++m) {
+            lx += fd_weight<H>(m) * (p1[j + m] + p1[j - m]);
+            lz += fd_weight<H>(m) * (p1[j + m * P] + p1[j - m * P]);
+        }
+        d += cj.beta * 2.0f * v * g.dt * g.dt * (lx * rdx2 + lz * rdz2);
+    }
+    if (cj.nb) {
+        const float s = vdt[j] / g.dx;
+        const Taps t = taps_of(s);
+        const float u11 = (2.0f * s - 3.0f) * 0.5f, u12 = 2.0f - 2.0f * s, u13 = (2.0f * s - 1.0f) * 0.5f;  // dt/ds
+        for (int bb = 0; bb < cj.nb; ++bb) {
+            const long long sp = cj.dir[bb] == 0 ? P : cj.dir[bb] == 1 ? -P : cj.dir[bb] == 2 ? 1 : -1;
+            const float dE = 2.0f * (u11 * p1[j] + u12 * p1[j + sp] + u13 * p1[j + 2 * sp]) -
+                             2.0f * t.t11 * u11 * p0[j] - 2.0f * (u11 * t.t12 + t.t11 * u12) * p0[j + sp] -
+                             2.0f * (t.t12 * u12 + u11 * t.t13 + t.t11 * u13) * p0[j + 2 * sp] -
+                             2.0f * (u12 * t.t13 + t.t12 * u13) * p0[j + 3 * sp] -
+                             2.0f * t.t13 * u13 * p0[j + 4 * sp];
+            d += cj.gam[bb] * dE * g.dt / g.dx;
+        }
+    }
+    if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * g.dt * v;
+    b.gpad[(long long)inst * g.fstride + j] += out * d;
+}
+
+// grad[s][cell] = sum over shots and over the padded cells that replicate
+// the interior cell (get_velp is a clamp, fdtd2D_modelling.c:1187-1238),
+// summed in double.
+__global__ void k_reduce_exact(const Geom g, const float *__restrict__ gpad, float *__restrict__ grad,
+                               int nsamples)
+{
+    const long long cells = (long long)g.nz * g.nx;
+    const long long total = (long long)nsamples * cells;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(e / cells);
+        const long long kk = e - (long long)s * cells;
+        const int jz = (int)(kk / g.nx), jx = (int)(kk - (long long)jz * g.nx);
+        const int z0 = jz == 0 ? 0 : jz + g.pml, z1 = jz == g.nz - 1 ? g.ntz - 1 : jz + g.pml;
+        const int x0 = jx == 0 ? 0 : jx + g.pml, x1 = jx == g.nx - 1 ? g.ntx - 1 : jx + g.pml;
+        double acc = 0.0;
+        for (int shot = 0; shot < g.ns; ++shot) {
+            const float *gp = gpad + ((long long)s * g.ns + shot) * g.fstride;
+            for (int iz = z0; iz <= z1; ++iz)
+                for (int ix = x0; ix <= x1; ++ix) acc += (double)gp[(long long)iz * g.pitch + ix + g.xoff];
+        }
+        grad[e] = (float)acc;
+    }
+}
+
+}  // namespace gbfwi

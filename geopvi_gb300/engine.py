@@ -95,7 +95,8 @@ class Fwi2dEngine:
         """One workspace is held at a time; it is sized once per batch shape
         (the resident count is not re-derived from free memory while the
         engine's own workspace occupies part of it)."""
-        key = (nsamples, flags & (_native.FLAG_FORWARD_ONLY | _native.FLAG_CHECKPOINT | _native.FLAG_PLAIN))
+        key = (nsamples, flags & (_native.FLAG_FORWARD_ONLY | _native.FLAG_CHECKPOINT | _native.FLAG_PLAIN |
+                                  _native.FLAG_EXACT_GRADIENT))
         if self._work_key != key:
             self._work = None
             self._work_key = None
@@ -113,11 +114,13 @@ class Fwi2dEngine:
     # ---- solve ----
     def run(self, vel: torch.Tensor, obs: torch.Tensor, *, imaging: bool = False,
             want_grad: bool = True, want_syn: bool = False, forward_only: bool = False,
-            profile: bool = False, out: dict | None = None) -> RunResult:
+            profile: bool = False, exact: bool = False, out: dict | None = None) -> RunResult:
         """vel (n, nz*nx) float32 CUDA; obs (ns*nt*nr,) float32 CUDA.
 
         Returns misfit (n,) float64, grad (n, nz*nx) float32 in the reference's
         scaling (the array fwi_2D accumulates), syn (n, ns*nt*nr) if asked.
+        ``exact=True`` returns instead grad = dJ/dv of the misfit J, the exact
+        discrete adjoint of the scheme (no counterpart in the reference).
         Outputs are reused across calls of the same shape unless ``out`` is given.
         """
         p = self.params
@@ -141,6 +144,10 @@ class Fwi2dEngine:
             flags |= _native.FLAG_PROFILE
         elif self.graph and not self.plain:
             flags |= _native.FLAG_GRAPH
+        if exact:
+            if imaging:
+                raise ValueError("the exact gradient is defined for the FWI misfit, not for imaging")
+            flags |= _native.FLAG_EXACT_GRADIENT
         if forward_only:
             flags |= _native.FLAG_FORWARD_ONLY
             want_grad = False

@@ -49,7 +49,7 @@ class ForwardModel(Function):
 class Posterior:
     def __init__(self, data, config, vel_fixed=1950, sigma=0.1, num_processes=1,
                  log_prior=None, mask=None, paramfile="input_params.txt", device=None,
-                 max_resident=None, hbm_budget=None, graph=True):
+                 max_resident=None, hbm_budget=None, graph=True, gradient="reference"):
         """
         data: observed data with shape (ns*nt*nr,), float32
         config: configparser with the ``[FWI]`` section of the example's config.ini
@@ -60,7 +60,14 @@ class Posterior:
         mask: boolean array (nz*nx,) -- cells with mask = False are fixed
         paramfile: the positional parameter file written from ``config``
         device / max_resident / hbm_budget / graph: engine placement and sizing
+        gradient: "reference" -- the reference's gradient (backward_IO's
+            imaging-condition approximation, in its scaling); "exact" -- dJ/dv
+            of the misfit, the exact discrete adjoint of the scheme, which a
+            finite difference of ``fwi``'s loss converges to
         """
+        if gradient not in ("reference", "exact"):
+            raise ValueError(f"gradient must be 'reference' or 'exact', not {gradient!r}")
+        self.gradient = gradient
         self.data = data
         self.log_prior = log_prior
         self.num_processes = num_processes
@@ -91,7 +98,7 @@ class Posterior:
         """vel: full model (nz*nx,) float64 -> (loss, -grad[mask])."""
         vel = torch.as_tensor(np.asarray(vel, dtype=np.float64)).to(self.device)
         loss, grad = self._run(vel.to(torch.float32).unsqueeze(0))
-        return float(loss[0].item()), -grad[0][self._mask_dev].double().cpu().numpy()
+        return float(loss[0].item()), grad[0][self._mask_dev].double().cpu().numpy()
 
     def _full_models(self, x: torch.Tensor) -> torch.Tensor:
         m = x.shape[0]
@@ -100,8 +107,10 @@ class Posterior:
         return vel.to(torch.float32)
 
     def _run(self, vel32: torch.Tensor):
-        r = self.engine.run(vel32.contiguous(), self._obs, want_grad=True)
-        return r.misfit, r.grad
+        """(loss, d loss / d vel): the reference's -grad, or the exact dJ/dv."""
+        exact = self.gradient == "exact"
+        r = self.engine.run(vel32.contiguous(), self._obs, want_grad=True, exact=exact)
+        return r.misfit, (r.grad if exact else -r.grad)
 
     # ---- batched form (posterior.py:112-149) ----
     def fwi(self, x):
@@ -109,7 +118,7 @@ class Posterior:
         on_device = isinstance(x, torch.Tensor) and x.is_cuda
         xt = torch.as_tensor(x.detach() if isinstance(x, torch.Tensor) else np.asarray(x, dtype=np.float64))
         loss, grad = self._run(self._full_models(xt))
-        g = -grad[:, self._mask_dev].to(torch.float64)
+        g = grad[:, self._mask_dev].to(torch.float64)
         loss = loss.clone()
         if on_device:
             return loss, g

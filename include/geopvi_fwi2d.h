@@ -59,6 +59,11 @@ typedef struct gb_fwi2d_params {
                                     stored-field memory; results identical to full storage */
 #define GB_FWI2D_FORWARD_ONLY 0x10u /* synthetic data only (forward_2D): no adjoint, no stored field */
 #define GB_FWI2D_PROFILE 0x20u   /* time the step-kernel loops with CUDA events (not with GRAPH) */
+#define GB_FWI2D_EXACT_GRADIENT 0x40u /* grad = dJ/dv of J = 0.5*sum((syn-obs)^2), the exact discrete
+                                        adjoint of the FD scheme (FP32), instead of backward_IO's
+                                        gradient.  No counterpart in the reference.  Not with IMAGING;
+                                        with CHECKPOINT the forward levels are kept per ~sqrt(nt)-step
+                                        segment instead of for all nt steps */
 
 /* read_parameters (fdtd2D_modelling.c:1328): parse the positional file. */
 int gb_fwi2d_read_params(const char *path, gb_fwi2d_params *out);

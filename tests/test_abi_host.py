@@ -169,3 +169,19 @@ def test_arena_first_fit_and_merge():
     a.release(0, 3 * 256)
     a.release(z, 1000)
     assert a.free == [(0, 10 * 256)]
+
+
+def test_exact_gradient_workspace_and_flags(engine_lib):
+    from geopvi_gb300 import workloads
+    p = workloads.cfg3().params  # nt 4000: all levels vs one ~64-step segment
+    cp = p.c()
+    full = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 4, _native.FLAG_EXACT_GRADIENT)
+    seg = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 4,
+                                              _native.FLAG_EXACT_GRADIENT | _native.FLAG_CHECKPOINT)
+    assert 0 < seg * 10 < full
+    # every forward level of every resident solve is kept
+    assert full >= 4 * 4 * p.nt * p.ntp
+    small = cases.SMALL["fwi_o8"]["params"].c()
+    st = engine_lib.gb_fwi2d_batch(ctypes.byref(small), 1, 1, 1, None, None, None,
+                                   _native.FLAG_EXACT_GRADIENT | _native.FLAG_IMAGING, 0, 1, 1 << 30, None)
+    assert st == _native.EINVAL
