@@ -97,6 +97,22 @@ GBX_HD float div_fast(float x, float y, float r)
     return gbx_copysign(gbx_fma(rem, r, q0), x);
 }
 
+// -(x / y) correctly rounded, from div_fast's three operations with r
+// negated (nr = -r): n0 = RN(x*nr) = -q0, RN(n0*y + x) is Markstein's
+// remainder, and RN(rem*nr + n0) = -RN(q0 + rem*r) since rounding to nearest
+// is symmetric.  For x = +-0 the steps give the zero of the opposite sign,
+// which is the negated quotient, so no sign fix-up is needed.
+GBX_HD float div_fast_neg(float x, float y, float nr)
+{
+    const float n0 = gbx_mul(x, nr);
+    return gbx_fma(gbx_fma(n0, y, x), nr, n0);
+}
+
+// (x / y) / y with both divisions on the fast path: two negated quotients
+// give the quotient with its sign (zeros included).  Valid for x = 0 and
+// kDiv2Lo <= |x| <= kDiv2Hi.
+GBX_HD float div2_fast(float x, float y, float nr) { return div_fast_neg(div_fast_neg(x, y, nr), y, nr); }
+
 // True when v is zero or lo <= |v| <= hi (NaN: false).
 GBX_HD bool in_fast_range(float v, float lo, float hi)
 {
@@ -104,17 +120,49 @@ GBX_HD bool in_fast_range(float v, float lo, float hi)
     return (a <= hi) & ((a >= lo) | (a == 0.0f));
 }
 
+// The quotient Q = qs + rs / y (y > 0) -- qs = RN(xs / y) normal with
+// |qs| < 2^-62, rs = xs - qs*y its exact remainder -- rounded to nearest
+// even on the grid G = 2^-85, returned as the float Q * 2^-64 (a subnormal,
+// or the smallest normal 2^-126).  With |qs| = m * 2^(e-150) (m the 24-bit
+// significand, e the biased exponent <= 64), Q / G = m / 2^s + rs/(y G),
+// s = 65 - e >= 1.  The G/2 midpoints lie on qs's own grid, so Q and qs are
+// on the same side of every midpoint, and when qs is a midpoint the sign of
+// rs tells on which side Q lies (rs = 0: an exact tie, to even).  The
+// result's bit pattern is sign | N, N = the rounded multiple of G.
+GBX_HD float round_scaled_to_subnormal(float qs, float rs)
+{
+    const uint32_t b = gbx_bits(qs);
+    const uint32_t sign = b & 0x80000000u;
+    const int s = 65 - (int)((b >> 23) & 0xFFu);
+    if (s > 25) return gbx_from_bits(sign);  // |Q| < G/4: rounds to zero
+    const uint32_t m = (b & 0x7FFFFFu) | 0x800000u;
+    const uint32_t qint = m >> s, rem = m & ((1u << s) - 1u), half = 1u << (s - 1);
+    uint32_t n = qint;
+    if (rem > half) {
+        n += 1u;
+    } else if (rem == half) {
+        if (rs == 0.0f)
+            n += qint & 1u;
+        else if (((gbx_bits(rs) ^ b) & 0x80000000u) == 0u)  // |Q| > |qs|
+            n += 1u;
+    }
+    return gbx_from_bits(sign | n);
+}
+
 // x / y correctly rounded for every x (y > 0).  On the proved range: the
-// fast path.  Below it (|x| < 2^-100, including subnormals): x * 2^64 is
-// exact and lands inside the range, and scaling the quotient back by 2^-64
-// is exact whenever the result is normal, |q * 2^-64| >= 2^-126; only
-// quotients in the subnormal range, and huge or non-finite x, take IEEE
-// division.
+// fast path.  Below it (|x| < 2^-100, including subnormals): xs = x * 2^64 is
+// exact and lands inside the range; scaling the quotient back by 2^-64 is
+// exact whenever the result is normal, |q * 2^-64| >= 2^-126, and a quotient
+// in the subnormal range is rounded on the subnormal grid from the scaled
+// quotient and its exact remainder.  Only huge or non-finite x (and divisors
+// the host could not prove) take IEEE division.
 GBX_COLD float div_const_slow(float x, float y, float r, int fast)
 {
     if (fast && std::fabs(x) < kDivLo) {
-        const float qs = div_fast(gbx_mul(x, 0x1p64f), y, r);
+        const float xs = gbx_mul(x, 0x1p64f);
+        const float qs = div_fast(xs, y, r);
         if (std::fabs(qs) >= 0x1p-62f) return gbx_mul(qs, 0x1p-64f);
+        return round_scaled_to_subnormal(qs, gbx_fma(-qs, y, xs));
     }
     return gbx_div(x, y);
 }
@@ -134,8 +182,27 @@ GBX_COLD float div_const2_slow(float x, float y, float r, int fast)
 
 GBX_HD float div_const2(float x, float y, float r, int fast)
 {
-    if (fast && in_fast_range(x, kDiv2Lo, kDiv2Hi)) return div_fast(div_fast(x, y, r), y, r);
+    if (fast && in_fast_range(x, kDiv2Lo, kDiv2Hi)) return div2_fast(x, y, -r);
     return div_const2_slow(x, y, r, fast);
+}
+
+// (x / y) / y for the lanes that miss div2_fast's range, inline for the
+// common case: nonzero |x| < 2^-80 (the decaying tails ahead of a
+// wavefront).  xs = x * 2^64 is exact and inside div_fast's range; the two
+// scaled quotients equal the unscaled ones times 2^64 whenever the unscaled
+// ones are normal (|q| >= 2^-62 scaled), and the final * 2^-64 is then exact.
+// Quotients in the subnormal range, huge x and non-finite x take
+// div_const2_slow (IEEE division where needed).
+GBX_HD float div2_any(float x, float y, float r, int fast)
+{
+    const float ax = std::fabs(x);
+    if (fast && ax < kDiv2Lo && ax != 0.0f) {
+        const float nr = -r;
+        const float q1 = div_fast_neg(gbx_mul(x, 0x1p64f), y, nr);  // -(x/y) * 2^64
+        const float q2 = div_fast_neg(q1, y, nr);                   // (x/y/y) * 2^64
+        if (std::fabs(q1) >= 0x1p-62f && std::fabs(q2) >= 0x1p-62f) return gbx_mul(q2, 0x1p-64f);
+    }
+    return div_const2(x, y, r, fast);
 }
 
 // Split of 1 - w into floats bh + bl (exact) for the boundary blend, with
@@ -161,11 +228,11 @@ struct BlendCoef {
 // formula is evaluated (rare: near-ties, cancellation, extreme magnitudes).
 GBX_COLD float blend_mix_double(float a, float q, double omw) { return gbx_d2f(gbx_dmix(a, omw, q)); }
 
-GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
+// The FP32 evaluation below for 2^-60 <= |q| <= 2^60, |a| <= 2^60: true and
+// the result in *out when its rounding is proved, false otherwise.
+GBX_HD bool blend_mix_fp32(float a, float q, const BlendCoef &c, float *out)
 {
-    if (q == 0.0f) return gbx_add(a, gbx_mul(c.bh, q));  // a + (+-0), signs as in double
-    const float aq = std::fabs(q), aa = std::fabs(a);
-    if (fp32_ok && aq >= 0x1p-60f && aq <= 0x1p60f && aa <= 0x1p60f) {
+    {
         const float ph = gbx_mul(c.bh, q);
         const float pl = gbx_fma(c.bh, q, -ph);
         const float qh = gbx_mul(c.bl, q);
@@ -186,10 +253,37 @@ GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
             const uint32_t ex = (rb >> 23) & 0xFFu;
             const uint32_t hu_ex = ex - ((rb & 0x7FFFFFu) ? 24u : 25u);  // half ulp (below, if r = 2^k)
             const float hu = gbx_from_bits(hu_ex << 23);
-            if (gbx_add(std::fabs(d), err) < gbx_mul(hu, 0.99f)) return r;
+            if (gbx_add(std::fabs(d), err) < gbx_mul(hu, 0.99f)) {
+                *out = r;
+                return true;
+            }
         }
     }
+    return false;
+}
+
+// Tiny operands (|q| < 2^-60, |a| < 2^-40, the tails ahead of a wavefront):
+// a * 2^100 and q * 2^100 are exact and inside the FP32 evaluation's range,
+// and RN_f(RN_d(X * 2^100)) = RN_f(RN_d(X)) * 2^100 whenever the unscaled
+// result is normal (|r| >= 2^-26 scaled), so the scaled result times 2^-100
+// is exact.  Subnormal results, and anything else unproved, take the double
+// formula.
+GBX_COLD float blend_mix_rare(float a, float q, const BlendCoef &c, int fp32_ok)
+{
+    float r;
+    if (fp32_ok && std::fabs(q) < 0x1p-60f && std::fabs(a) < 0x1p-40f &&
+        blend_mix_fp32(gbx_mul(a, 0x1p100f), gbx_mul(q, 0x1p100f), c, &r) && std::fabs(r) >= 0x1p-26f)
+        return gbx_mul(r, 0x1p-100f);
     return blend_mix_double(a, q, c.omw);
+}
+
+GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
+{
+    if (q == 0.0f) return gbx_add(a, gbx_mul(c.bh, q));  // a + (+-0), signs as in double
+    const float aq = std::fabs(q), aa = std::fabs(a);
+    float r;
+    if (fp32_ok && aq >= 0x1p-60f && aq <= 0x1p60f && aa <= 0x1p60f && blend_mix_fp32(a, q, c, &r)) return r;
+    return blend_mix_rare(a, q, c, fp32_ok);
 }
 
 }  // namespace gbfwi

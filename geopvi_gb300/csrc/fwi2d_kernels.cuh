@@ -226,15 +226,15 @@ struct TileShape {
 };
 
 // Exact two-step quotients (x/d)/d for both Laplacian terms; one range test
-// covers the four divisions of a cell, the rare rest takes div_const2.
+// covers the four divisions of a cell, the rest takes div2_any.
 __device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Geom &g, float &ddx, float &ddz)
 {
     if (g.fast_dx & g.fast_dz & in_fast_range(lx, kDiv2Lo, kDiv2Hi) & in_fast_range(lz, kDiv2Lo, kDiv2Hi)) {
-        ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
-        ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
+        ddx = div2_fast(lx, g.dx, -g.rdx);
+        ddz = div2_fast(lz, g.dz, -g.rdz);
     } else {
-        ddx = div_const2(lx, g.dx, g.rdx, g.fast_dx);
-        ddz = div_const2(lz, g.dz, g.rdz, g.fast_dz);
+        ddx = div2_any(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div2_any(lz, g.dz, g.rdz, g.fast_dz);
     }
 }
 
@@ -256,7 +256,7 @@ struct WarpCtx {
 // exact quotients, the new level and the snapshot (forward) or gradient
 // term (adjoint).  The exact-quotient range tests are warp votes, so the
 // common case is one uniform branch; lanes outside the fast range (zeros
-// and tiny tails included in div_const2's scaling) fix their quotients.
+// and tiny tails, which div2_any scales inline) fix their quotients.
 template <int H, bool ADJ>
 __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const float (&win)[2 * H + 1],
                                          const float *srow, float p0c, float vd, float *p2, float *ps, float *G)
@@ -271,11 +271,11 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
     }
     const bool ok = (g.fast_dx & g.fast_dz) && in_fast_range(lx, kDiv2Lo, kDiv2Hi) &&
                     in_fast_range(lz, kDiv2Lo, kDiv2Hi);
-    float ddx = div_fast(div_fast(lx, g.dx, g.rdx), g.dx, g.rdx);
-    float ddz = div_fast(div_fast(lz, g.dz, g.rdz), g.dz, g.rdz);
+    float ddx = div2_fast(lx, g.dx, -g.rdx);
+    float ddz = div2_fast(lz, g.dz, -g.rdz);
     if (!__all_sync(0xffffffffu, ok) && !ok) {
-        ddx = div_const2_slow(lx, g.dx, g.rdx, g.fast_dx);
-        ddz = div_const2_slow(lz, g.dz, g.rdz, g.fast_dz);
+        ddx = div2_any(lx, g.dx, g.rdx, g.fast_dx);
+        ddz = div2_any(lz, g.dz, g.rdz, g.fast_dz);
     }
     const float q = fa(fs(fm(2.0f, p1c), p0c), fm(fm(vd, vd), fa(ddx, ddz)));
     *p2 = q;
@@ -285,8 +285,8 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
             if (!b.imaging) {
                 const float x = fa(fs(q, fm(2.0f, p1c)), p0c);
                 const bool okt = g.fast_dt && in_fast_range(x, kDiv2Lo, kDiv2Hi);
-                v = div_fast(div_fast(x, g.dt, g.rdt), g.dt, g.rdt);
-                if (!__all_sync(0xffffffffu, okt) && !okt) v = div_const2_slow(x, g.dt, g.rdt, g.fast_dt);
+                v = div2_fast(x, g.dt, -g.rdt);
+                if (!__all_sync(0xffffffffu, okt) && !okt) v = div2_any(x, g.dt, g.rdt, g.fast_dt);
             }
             *ps = v;
         } else {
@@ -448,7 +448,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
         if (w.ps && iz >= g.pml && iz < g.ntz - g.pml) {
             const long long pc = (long long)(iz - g.pml) * g.ipitch;
             if (!ADJ)
-                w.ps[pc] = b.imaging ? q : div_const2(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+                w.ps[pc] = b.imaging ? q : div2_any(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
             else
                 w.G[pc] = fa(w.G[pc], fm(w.ps[pc], q));
         }

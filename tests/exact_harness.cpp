@@ -76,6 +76,60 @@ long long harness_div_fast_binades(float y, int klo, int khi)
     return bad;
 }
 
+// div2_any against (x / y) / y bit for bit: every 7th significand of each
+// binade from the subnormals up to 2^-79 and of a few normal binades, both
+// signs, plus zeros, every 37th subnormal and huge values.
+long long harness_div2_any(float y)
+{
+    const float r = 1.0f / y;
+    long long bad = 0;
+    auto check = [&](float x) {
+        const float a = div2_any(x, y, r, 1), b = (x / y) / y;
+        if (std::memcmp(&a, &b, 4) != 0) ++bad;
+    };
+    for (int k = -126; k <= -79; ++k)
+        for (uint32_t m = 0; m < (1u << 23); m += 7) {
+            const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
+            float x;
+            std::memcpy(&x, &bits, 4);
+            check(x);
+            check(-x);
+        }
+    for (uint32_t sub = 1; sub < (1u << 23); sub += 37) {
+        float x;
+        std::memcpy(&x, &sub, 4);
+        check(x);
+        check(-x);
+    }
+    for (float x : {0.0f, -0.0f, 1.0f, -3.5f, 1e30f, -3e38f, 0x1p81f})
+        check(x);
+    return bad;
+}
+
+// div2_fast (two negated quotients, no sign fix-up) against (x / y) / y bit
+// for bit, every significand of the binades 2^k, k in [klo, khi], both
+// signs, and both zeros.
+long long harness_div2_fast_binades(float y, int klo, int khi)
+{
+    const float nr = -(1.0f / y);
+    long long bad = 0;
+    auto check = [&](float x) {
+        const float a = div2_fast(x, y, nr), b = (x / y) / y;
+        if (std::memcmp(&a, &b, 4) != 0) ++bad;
+    };
+    for (int k = klo; k <= khi; ++k)
+        for (uint32_t m = 0; m < (1u << 23); ++m) {
+            const uint32_t bits = ((uint32_t)(127 + k) << 23) | m;
+            float x;
+            std::memcpy(&x, &bits, 4);
+            check(x);
+            check(-x);
+        }
+    check(0.0f);
+    check(-0.0f);
+    return bad;
+}
+
 static float ref_mix(float a, double omw, float q) { return (float)((double)a + omw * (double)q); }
 
 // Random and adversarial trials of blend_mix against the double formula.
@@ -103,6 +157,14 @@ long long harness_blend_mismatches(int pml0, long long trials, unsigned seed, lo
             if (t % 89 == 4) q = -0.0f;
             if (t % 83 == 5) ext = 0.0f;
             if (t % 79 == 6) q = 1e-41f;  // subnormal
+            if (t % 7 == 5) {  // tiny tails: the scaled FP32 path
+                q = std::ldexp(q, -95);
+                ext = std::ldexp(ext, -95);
+            }
+            if (t % 13 == 9) {  // results near and below the normal range
+                q = std::ldexp(q, -118);
+                ext = std::ldexp(ext, -118);
+            }
             const float a = c.w * ext;
             // near-tie construction: choose q so that a + omw*q sits near a float midpoint
             if (t % 4 == 3 && c.omw > 0) {

@@ -25,6 +25,10 @@ def harness(tmp_path_factory):
     L.harness_div_mismatches.restype = ctypes.c_longlong
     L.harness_div_fast_binades.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
     L.harness_div_fast_binades.restype = ctypes.c_longlong
+    L.harness_div2_any.argtypes = [ctypes.c_float]
+    L.harness_div2_any.restype = ctypes.c_longlong
+    L.harness_div2_fast_binades.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
+    L.harness_div2_fast_binades.restype = ctypes.c_longlong
     L.harness_blend_mismatches.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
                                            ctypes.POINTER(ctypes.c_longlong)]
     L.harness_blend_mismatches.restype = ctypes.c_longlong
@@ -41,6 +45,21 @@ def test_fast_quotient_at_the_ends_of_its_range(harness, y):
     # the fast path's proved range is 2^-100 <= |x| <= 2^100 (binades -100 and 99 are its ends)
     assert harness.harness_div_fast_binades(y, -100, -99) == 0
     assert harness.harness_div_fast_binades(y, 98, 99) == 0
+
+
+@pytest.mark.parametrize("y", [10.0, 12.0, 1e-3, 8e-4])
+def test_two_step_quotient_without_sign_fixup(harness, y):
+    """div2_fast: (x/y)/y from two negated quotients, signed zeros included,
+    over the ends of its range (2^-80 .. 2^80) and a middle binade."""
+    assert harness.harness_div2_fast_binades(y, -80, -80) == 0
+    assert harness.harness_div2_fast_binades(y, 0, 0) == 0
+    assert harness.harness_div2_fast_binades(y, 79, 79) == 0
+
+
+@pytest.mark.parametrize("y", [10.0, 12.0, 9.0, 1e-3, 8e-4, 2.0 ** -20, 2.0 ** 20])
+def test_two_step_quotient_of_tiny_values(harness, y):
+    """div2_any: the inline scaled path for |x| < 2^-80, IEEE below it."""
+    assert harness.harness_div2_any(y) == 0
 
 
 @pytest.mark.parametrize("pml0", [1, 5, 10, 20, 30])
