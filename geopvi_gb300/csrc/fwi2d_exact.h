@@ -186,21 +186,30 @@ GBX_HD float div_const2(float x, float y, float r, int fast)
     return div_const2_slow(x, y, r, fast);
 }
 
-// (x / y) / y for the lanes that miss div2_fast's range, inline for the
-// common case: nonzero |x| < 2^-80 (the decaying tails ahead of a
-// wavefront).  xs = x * 2^64 is exact and inside div_fast's range; the two
-// scaled quotients equal the unscaled ones times 2^64 whenever the unscaled
-// ones are normal (|q| >= 2^-62 scaled), and the final * 2^-64 is then exact.
-// Quotients in the subnormal range, huge x and non-finite x take
-// div_const2_slow (IEEE division where needed).
+// x / y for 0 < |x| < 2^-80 (y in the proved divisor range), correctly
+// rounded including quotients in the subnormal range: xs = x * 2^64 is exact
+// and inside div_fast's range; a normal quotient is the scaled one times
+// 2^-64 (exact), a subnormal one is rounded on the subnormal grid from the
+// scaled quotient and its exact remainder.  nr = -RN(1/y).
+GBX_HD float div_tiny(float x, float y, float nr)
+{
+    const float xs = gbx_mul(x, 0x1p64f);
+    const float n = div_fast_neg(xs, y, nr);  // -RN(xs / y)
+    if (std::fabs(n) >= 0x1p-62f) return gbx_mul(n, -0x1p-64f);
+    return round_scaled_to_subnormal(-n, gbx_fma(n, y, xs));
+}
+
+// (x / y) / y for the lanes that miss div2_fast's range, inline for every
+// nonzero |x| < 2^-80 (the decaying tails ahead of a wavefront, down to
+// subnormals); huge and non-finite x take div_const2's slow path.
 GBX_HD float div2_any(float x, float y, float r, int fast)
 {
     const float ax = std::fabs(x);
     if (fast && ax < kDiv2Lo && ax != 0.0f) {
         const float nr = -r;
-        const float q1 = div_fast_neg(gbx_mul(x, 0x1p64f), y, nr);  // -(x/y) * 2^64
-        const float q2 = div_fast_neg(q1, y, nr);                   // (x/y/y) * 2^64
-        if (std::fabs(q1) >= 0x1p-62f && std::fabs(q2) >= 0x1p-62f) return gbx_mul(q2, 0x1p-64f);
+        const float q1 = div_tiny(x, y, nr);
+        if (q1 == 0.0f) return q1;  // +-0 / y
+        return std::fabs(q1) < kDiv2Lo ? div_tiny(q1, y, nr) : gbx_mul(div_fast_neg(q1, y, nr), -1.0f);
     }
     return div_const2(x, y, r, fast);
 }
@@ -262,28 +271,24 @@ GBX_HD bool blend_mix_fp32(float a, float q, const BlendCoef &c, float *out)
     return false;
 }
 
-// Tiny operands (|q| < 2^-60, |a| < 2^-40, the tails ahead of a wavefront):
-// a * 2^100 and q * 2^100 are exact and inside the FP32 evaluation's range,
-// and RN_f(RN_d(X * 2^100)) = RN_f(RN_d(X)) * 2^100 whenever the unscaled
-// result is normal (|r| >= 2^-26 scaled), so the scaled result times 2^-100
-// is exact.  Subnormal results, and anything else unproved, take the double
-// formula.
-GBX_COLD float blend_mix_rare(float a, float q, const BlendCoef &c, int fp32_ok)
-{
-    float r;
-    if (fp32_ok && std::fabs(q) < 0x1p-60f && std::fabs(a) < 0x1p-40f &&
-        blend_mix_fp32(gbx_mul(a, 0x1p100f), gbx_mul(q, 0x1p100f), c, &r) && std::fabs(r) >= 0x1p-26f)
-        return gbx_mul(r, 0x1p-100f);
-    return blend_mix_double(a, q, c.omw);
-}
-
 GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)
 {
     if (q == 0.0f) return gbx_add(a, gbx_mul(c.bh, q));  // a + (+-0), signs as in double
-    const float aq = std::fabs(q), aa = std::fabs(a);
+    // Tiny operands (|q| < 2^-60, |a| < 2^-40: the tails ahead of a
+    // wavefront) are scaled by 2^100 first.  a * 2^100 and q * 2^100 are exact
+    // and inside the FP32 evaluation's range, and RN_f(RN_d(X * 2^100)) =
+    // RN_f(RN_d(X)) * 2^100 whenever the unscaled result is normal (|r| >=
+    // 2^-26 scaled), so scaling back is exact.  Subnormal results, and
+    // anything else unproved, take the double formula.
+    const bool tiny = std::fabs(q) < 0x1p-60f && std::fabs(a) < 0x1p-40f;
+    const float up = tiny ? 0x1p100f : 1.0f, lo = tiny ? 0x1p-26f : 0.0f;
+    const float as = gbx_mul(a, up), qs = gbx_mul(q, up);
+    const float aq = std::fabs(qs);
     float r;
-    if (fp32_ok && aq >= 0x1p-60f && aq <= 0x1p60f && aa <= 0x1p60f && blend_mix_fp32(a, q, c, &r)) return r;
-    return blend_mix_rare(a, q, c, fp32_ok);
+    if (fp32_ok && aq >= 0x1p-60f && aq <= 0x1p60f && std::fabs(as) <= 0x1p60f && blend_mix_fp32(as, qs, c, &r) &&
+        std::fabs(r) >= lo)
+        return gbx_mul(r, tiny ? 0x1p-100f : 1.0f);
+    return blend_mix_double(a, q, c.omw);
 }
 
 }  // namespace gbfwi
