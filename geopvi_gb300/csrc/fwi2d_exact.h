@@ -232,9 +232,11 @@ struct BlendCoef {
 // |t| <= |s|/4, s - r is exact (Sterbenz), so d = RN((s - r) + t) is within
 // 3u*S + u*|d| of D.  The double rounding moves X by at most 2^-52*|r|.  If
 // |d| plus those bounds stays below half an ulp of r (the smaller one when r
-// is a power of two), every value between X and RN_d(X) rounds to r, which
-// is then the reference's result.  Otherwise -- zeros aside -- the double
-// formula is evaluated (rare: near-ties, cancellation, extreme magnitudes).
+// is a power of two) -- tested against hu * (1 - 2^-16), which absorbs the
+// rounding of the test's own three additions -- every value between X and
+// RN_d(X) rounds to r, which is then the reference's result.  Otherwise --
+// zeros aside -- the double formula is evaluated (rare: X within ~2^-16 of a
+// half ulp from a midpoint, cancellation, extreme magnitudes).
 GBX_COLD float blend_mix_double(float a, float q, double omw) { return gbx_d2f(gbx_dmix(a, omw, q)); }
 
 // The FP32 evaluation below for 2^-60 <= |q| <= 2^60, |a| <= 2^60: true and
@@ -262,9 +264,32 @@ GBX_HD bool blend_mix_fp32(float a, float q, const BlendCoef &c, float *out)
             const uint32_t ex = (rb >> 23) & 0xFFu;
             const uint32_t hu_ex = ex - ((rb & 0x7FFFFFu) ? 24u : 25u);  // half ulp (below, if r = 2^k)
             const float hu = gbx_from_bits(hu_ex << 23);
-            if (gbx_add(std::fabs(d), err) < gbx_mul(hu, 0.99f)) {
+            if (gbx_add(std::fabs(d), err) < gbx_mul(hu, 0x1.fffep-1f)) {  // hu * (1 - 2^-16)
                 *out = r;
                 return true;
+            }
+            // Exact ties.  When 1 - w has few significant bits (w = 0.5, 0.75,
+            // ...), X often sits exactly on the midpoint M = r + sign(d)*hu.
+            // With bl*q = 0, X = a + ph + pl exactly and X - M = e + pl + k,
+            // k = (s - r) - sign(d)*hu exact (r is s or a neighbour of s when
+            // |t| <= 2^-20 |s|, so k is a sum of two nearby powers of two).
+            // Two-sums decide whether that is zero; an exact midpoint is a
+            // double, so the reference rounds it half to even.
+            if (qh == 0.0f && ql == 0.0f && std::fabs(t) <= gbx_mul(0x1p-20f, std::fabs(s))) {
+                const float k = gbx_sub(gbx_sub(s, r), d > 0.0f ? hu : -hu);
+                const float u = gbx_add(e, pl);
+                const float ub = gbx_sub(u, e), ue = gbx_add(gbx_sub(e, gbx_sub(u, ub)), gbx_sub(pl, ub));
+                const float v = gbx_add(u, k);
+                const float vb = gbx_sub(v, u), ve = gbx_add(gbx_sub(u, gbx_sub(v, vb)), gbx_sub(k, vb));
+                if (ve == 0.0f && v == -ue) {
+                    if ((rb & 1u) == 0u) {
+                        *out = r;  // r is the even neighbour
+                    } else {       // the neighbour of r toward X
+                        const bool grows = (d > 0.0f) == (r > 0.0f);
+                        *out = gbx_from_bits(grows ? rb + 1u : rb - 1u);
+                    }
+                    return true;
+                }
             }
         }
     }

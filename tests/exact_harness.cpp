@@ -132,6 +132,37 @@ long long harness_div2_fast_binades(float y, int klo, int khi)
 
 static float ref_mix(float a, double omw, float q) { return (float)((double)a + omw * (double)q); }
 
+// Ties: operands with short significands, so that a + (1 - w) * q often
+// lands exactly on a float midpoint (weights 1/2, 3/4, 1/4, ... of pml0 = 4,
+// 8, 20).  Returns mismatches against the double formula; *fp32 counts the
+// trials the FP32 evaluation settled itself.
+long long harness_blend_ties(int pml0, long long trials, unsigned seed, long long *fp32)
+{
+    std::mt19937_64 rng(seed);
+    std::uniform_int_distribution<int> M(-(1 << 20), 1 << 20), E(-30, 10), B(20, 24);
+    long long bad = 0, ok32 = 0;
+    for (int i = 0; i < pml0; ++i) {
+        BlendCoef c;
+        c.w = (float)(1.0 - 1.0 * i / pml0);
+        c.omw = 1.0 - (double)c.w;
+        c.bh = (float)c.omw;
+        c.bl = (float)(c.omw - (double)c.bh);
+        for (long long t = 0; t < trials; ++t) {
+            const int e = E(rng);
+            const float q = std::ldexp((float)(M(rng) | 1) * (float)(1 << (24 - B(rng))), e - 20);
+            const float ext = std::ldexp((float)M(rng), e - 20 + (int)(t % 3) - 1);
+            const float a = c.w * ext;
+            float r32;
+            if (q != 0.0f && blend_mix_fp32(a, q, c, &r32)) ++ok32;
+            const float got = blend_mix(a, q, c, 1);
+            const float want = ref_mix(a, c.omw, q);
+            if (std::memcmp(&got, &want, 4) != 0) ++bad;
+        }
+    }
+    *fp32 = ok32;
+    return bad;
+}
+
 // Random and adversarial trials of blend_mix against the double formula.
 // Returns the number of bitwise mismatches; *fallbacks counts trials that took
 // the double path.

@@ -29,6 +29,9 @@ def harness(tmp_path_factory):
     L.harness_div2_any.restype = ctypes.c_longlong
     L.harness_div2_fast_binades.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int]
     L.harness_div2_fast_binades.restype = ctypes.c_longlong
+    L.harness_blend_ties.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
+                                     ctypes.POINTER(ctypes.c_longlong)]
+    L.harness_blend_ties.restype = ctypes.c_longlong
     L.harness_blend_mismatches.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
                                            ctypes.POINTER(ctypes.c_longlong)]
     L.harness_blend_mismatches.restype = ctypes.c_longlong
@@ -60,6 +63,16 @@ def test_two_step_quotient_without_sign_fixup(harness, y):
 def test_two_step_quotient_of_tiny_values(harness, y):
     """div2_any: the inline scaled path for |x| < 2^-80, IEEE below it."""
     assert harness.harness_div2_any(y) == 0
+
+
+@pytest.mark.parametrize("pml0", [4, 8, 20])
+def test_blend_exact_ties(harness, pml0):
+    """Weights whose 1 - w has few bits put the sum exactly on float midpoints;
+    the FP32 evaluation rounds those half to even itself."""
+    ok32 = ctypes.c_longlong(0)
+    trials = 20000
+    assert harness.harness_blend_ties(pml0, trials, 99 + pml0, ctypes.byref(ok32)) == 0
+    assert ok32.value >= 0.999 * pml0 * trials * 0.99  # nearly every nonzero trial settled in FP32
 
 
 @pytest.mark.parametrize("pml0", [1, 5, 10, 20, 30])
