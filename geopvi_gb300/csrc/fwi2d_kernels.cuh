@@ -41,6 +41,13 @@ constexpr int kThreads = kTileX * kWarps;   // 128
 
 // Resident blocks per SM the step kernel is compiled for (register cap
 // 65536 / (128 * this)); a build-time tuning knob.
+// Rows per block of the interior sweep (loads run one block ahead).  Two
+// measured faster than four: the unrolled row bodies, each with its inline
+// exact fallbacks, otherwise overflow the instruction cache.
+#ifndef GB_FWI2D_ROWS_U
+#define GB_FWI2D_ROWS_U 2
+#endif
+
 #ifndef GB_FWI2D_MIN_BLOCKS
 #define GB_FWI2D_MIN_BLOCKS 8
 #endif
@@ -298,14 +305,14 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
 // Interior sweep: every cell of the warp is inside the interior of the
 // padded grid, away from the absorbing strips, the source and the receivers,
 // so each row is lean_row without per-cell region tests.  Rows go in blocks
-// of kUnroll: the z window covers the block (2H + kUnroll values), the
+// of U = GB_FWI2D_ROWS_U: the z window covers the block (2H + U values), the
 // block's p0 / v*dt rows are fetched one block ahead, and the rows'
 // independent dependency chains interleave.
 template <int H, bool ADJ>
 __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
                                                float p0_first, float vd_first)
 {
-    constexpr int U = 4;
+    constexpr int U = GB_FWI2D_ROWS_U;
     static_assert(kWarpRows % U == 0, "row blocks must tile the warp's rows");
     float win[2 * H + U];
 #pragma unroll
