@@ -266,7 +266,8 @@ struct WarpCtx {
 // and tiny tails, which div2_any scales inline) fix their quotients.
 template <int H, bool ADJ>
 __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const float (&win)[2 * H + 1],
-                                         const float *srow, float p0c, float vd, float *p2, float *ps, float *G)
+                                         const float *srow, float p0c, float vd, float *p2, float *ps, float *G,
+                                         float psv, float gv)
 {
     const float p1c = win[H];
     float lx = fm(fd_weight<H>(0), p1c);
@@ -297,7 +298,7 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
             }
             *ps = v;
         } else {
-            *G = fa(*G, fm(*ps, q));
+            *G = fa(gv, fm(psv, q));  // psv = *ps, gv = *G, loaded ahead
         }
     }
 }
@@ -348,12 +349,24 @@ __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, co
                 vdn[u] = __ldg(vdt + (j0 + U + u) * pitch);
             }
         }
+        // Adjoint stored step: this block's snapshot and gradient values,
+        // requested before the stencil work that hides their latency.
+        float psv[U], gv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            psv[u] = gv[u] = 0.0f;
+            if (ADJ && ps) {
+                psv[u] = __ldg(ps + (long long)(j0 + u) * g.ipitch);
+                gv[u] = G[(long long)(j0 + u) * g.ipitch];
+            }
+        }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const float(&wu)[2 * H + 1] = *reinterpret_cast<const float(*)[2 * H + 1]>(win + u);
             float *psu = ps ? ps + (long long)(j0 + u) * g.ipitch : nullptr;
             float *Gu = (ADJ && ps) ? G + (long long)(j0 + u) * g.ipitch : nullptr;
-            lean_row<H, ADJ>(g, b, wu, scol + (j0 + u + H) * kBoxX, p0c[u], vd[u], p2 + (j0 + u) * pitch, psu, Gu);
+            lean_row<H, ADJ>(g, b, wu, scol + (j0 + u + H) * kBoxX, p0c[u], vd[u], p2 + (j0 + u) * pitch, psu, Gu,
+                             psv[u], gv[u]);
         }
 #pragma unroll
         for (int m = 0; m < 2 * H; ++m) win[m] = win[m + U];
