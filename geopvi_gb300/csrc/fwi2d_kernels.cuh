@@ -409,6 +409,13 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
             p0_next = __ldg(p0 + c + g.pitch);
             vd_next = __ldg(vdt + c + g.pitch);
         }
+        // Adjoint stored step: request the snapshot and gradient values early.
+        float psv = 0.0f, gv = 0.0f;
+        if (ADJ && w.ps && iz >= g.pml && iz < g.ntz - g.pml) {
+            const long long pc = (long long)(iz - g.pml) * g.ipitch;
+            psv = __ldg(w.ps + pc);
+            gv = w.G[pc];
+        }
         const float p1c = win[H];
         const int srow1 = (rr + H) * kBoxX;
         float q = p1c;  // cells the stencil skips keep the previous level
@@ -470,7 +477,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
             if (!ADJ)
                 w.ps[pc] = b.imaging ? q : div2_any(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
             else
-                w.G[pc] = fa(w.G[pc], fm(w.ps[pc], q));
+                w.G[pc] = fa(gv, fm(psv, q));
         }
         if (j + 1 < kWarpRows) {  // slide the z window one row down
 #pragma unroll
