@@ -10,6 +10,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+#include <cufft.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <cmath>
@@ -24,6 +26,7 @@
 #include "../../include/geopvi_fwi2d.h"
 #include "fwi2d_kernels.cuh"
 #include "fwi2d_exact_adjoint.cuh"
+#include "fwi2d_pstd.cuh"
 
 namespace gbfwi {
 
@@ -39,6 +42,7 @@ struct Derived {
     std::vector<float> rik;   // Ricker wavelet per time step
     std::vector<BlendCoef> coef;  // boundary weights w and 1 - w (fdtd2D_modelling.c:227-230)
     bool blend_fp32 = false;      // every (1 - w) * q is exact in double
+    std::vector<float> kk;        // pseudo-spectral mode: |k|^2 per padded cell, dense [ntz][ntx]
 };
 
 static int round_up(int v, int m) { return (v + m - 1) / m * m; }
@@ -81,8 +85,7 @@ static int validate(const gb_fwi2d_params &p)
     if (p.nx <= 0 || p.nz <= 0 || p.ns <= 0 || p.nt <= 0 || p.nr <= 0) return GB_FWI2D_EINVAL;
     if (p.pml0 <= 0 || p.nt_interval <= 0) return GB_FWI2D_EINVAL;
     if (!(p.dx > 0.0f) || !(p.dz > 0.0f) || !(p.dt > 0.0f) || !(p.f0 > 0.0f)) return GB_FWI2D_EINVAL;
-    if (p.laplace_solver == 1) return GB_FWI2D_ENOTSUP;  // pseudo-spectral Laplacian
-    if (p.laplace_solver != 0) return GB_FWI2D_EINVAL;
+    if (p.laplace_solver != 0 && p.laplace_solver != 1) return GB_FWI2D_EINVAL;
     if (p.Lc < 3 || p.Lc > 6) return GB_FWI2D_EINVAL;     // fd_coefficient: Lc+1 in 4..7
     if (p.nr > 1 && p.dr == 0) return GB_FWI2D_EINVAL;    // receivers would share one cell
     const long long Lc = p.Lc + 1, pml = p.pml0 + Lc;
@@ -148,6 +151,25 @@ static int significant_bits(double v)
     return n;
 }
 
+// wavenumber (fdtd2D_modelling.c:1127-1184): |k|^2 of the padded grid's DFT
+// bins.  dkx = 1/ntx/dx is stored as float; each component 2 pi dkx j (pi the
+// reference's 3.1415926, j = min(ix, ntx - ix) with the upper half starting
+// at ceil(ntx/2)) is stored as float; the squares are summed in double and
+// the sum stored as float.
+static void wavenumber(int ntx, int ntz, float dx, float dz, std::vector<float> &k)
+{
+    const float dkz = (float)(1.0 / ntz / dz), dkx = (float)(1.0 / ntx / dx);
+    const int ax = ntx / 2 * 2 < ntx ? ntx / 2 + 1 : ntx / 2;
+    const int az = ntz / 2 * 2 < ntz ? ntz / 2 + 1 : ntz / 2;
+    k.assign((size_t)ntx * ntz, 0.0f);
+    for (int iz = 0; iz < ntz; ++iz)
+        for (int ix = 0; ix < ntx; ++ix) {
+            const float kz = (float)(2 * kRefPi * dkz * (iz < az ? iz : ntz - iz));
+            const float kx = (float)(2 * kRefPi * dkx * (ix < ax ? ix : ntx - ix));
+            k[(size_t)iz * ntx + ix] = (float)((double)kx * (double)kx + (double)kz * (double)kz);
+        }
+}
+
 static int derive(const gb_fwi2d_params &p, Derived &d)
 {
     int st = validate(p);
@@ -191,6 +213,8 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.fast_dz = division_is_exact(p.dz) ? 1 : 0;
     g.fast_dt = division_is_exact(p.dt) ? 1 : 0;
     ricker(p.nt, p.dt, p.f0, d.rik);
+    g.pstd = p.laplace_solver == 1 ? 1 : 0;
+    if (g.pstd) wavenumber(g.ntx, g.ntz, p.dx, p.dz, d.kk);
     d.coef.resize(p.pml0);
     d.blend_fp32 = true;
     for (int i = 0; i < p.pml0; ++i) {
@@ -214,6 +238,7 @@ struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
     size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
     size_t store, lam, gpad;  // exact gradient only: forward levels, adjoint levels, padded dJ/dv
+    size_t spec;              // pseudo-spectral mode: [resident][ntz][ntx] complex double
     int resident;
     int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
 };
@@ -289,6 +314,8 @@ static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in
     L.syn = off;
     if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
     L.part = off;  off = align256(off + sizeof(double) * kMisfitBlocks * nsamples);
+    L.spec = off;
+    if (g.pstd) off = align256(off + sizeof(double2) * (size_t)g.ntz * g.ntx * resident);
     L.total = off;
     return L;
 }
@@ -495,15 +522,132 @@ static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, 
         k_step<H, false><<<grid, block, smem, st>>>(m.p1, g, b, sa);
 }
 
-static void step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
-                 cudaStream_t st)
+// ---------------------------------------------------------------------------
+// Pseudo-spectral mode: cuFFT, loaded on first use (the FD path needs no
+// FFT library), batched 2-D Z2Z plans cached per (device, grid, batch).
+// ---------------------------------------------------------------------------
+struct CufftApi {
+    decltype(&cufftPlanMany) plan_many = nullptr;
+    decltype(&cufftSetStream) set_stream = nullptr;
+    decltype(&cufftExecZ2Z) exec_z2z = nullptr;
+    decltype(&cufftDestroy) destroy = nullptr;
+};
+
+static const CufftApi *cufft_api()
 {
+    static CufftApi api;
+    static bool tried = false, ok = false;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (!tried) {
+        tried = true;
+        void *h = nullptr;
+        for (const char *name : {"libcufft.so.12", "libcufft.so", "/usr/local/cuda/lib64/libcufft.so.12"})
+            if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL)) != nullptr) break;
+        if (h) {
+            api.plan_many = (decltype(api.plan_many))dlsym(h, "cufftPlanMany");
+            api.set_stream = (decltype(api.set_stream))dlsym(h, "cufftSetStream");
+            api.exec_z2z = (decltype(api.exec_z2z))dlsym(h, "cufftExecZ2Z");
+            api.destroy = (decltype(api.destroy))dlsym(h, "cufftDestroy");
+            ok = api.plan_many && api.set_stream && api.exec_z2z && api.destroy;
+        }
+    }
+    return ok ? &api : nullptr;
+}
+
+static std::map<std::tuple<int, int, int, int>, cufftHandle> g_fft_plans;  // (device, ntz, ntx, batch)
+static std::map<std::tuple<int, int, int, uint32_t, uint32_t>, float *> g_kk_tables;  // (device, ntz, ntx, dx, dz)
+static thread_local int t_enqueue_error = 0;
+
+// A batched in-place 2-D double-complex plan for `batch` dense [ntz][ntx] arrays.
+static int fft_plan(const Geom &g, int batch, cufftHandle *out)
+{
+    const CufftApi *api = cufft_api();
+    if (!api) return GB_FWI2D_ENOTSUP;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    const auto key = std::make_tuple(dev, g.ntz, g.ntx, batch);
+    auto it = g_fft_plans.find(key);
+    if (it != g_fft_plans.end()) {
+        *out = it->second;
+        return GB_FWI2D_OK;
+    }
+    cufftHandle h;
+    int n[2] = {g.ntz, g.ntx};
+    const int dist = g.ntz * g.ntx;
+    if (api->plan_many(&h, 2, n, nullptr, 1, dist, nullptr, 1, dist, CUFFT_Z2Z, batch) != CUFFT_SUCCESS)
+        return GB_FWI2D_ENOMEM;
+    g_fft_plans[key] = h;
+    *out = h;
+    return GB_FWI2D_OK;
+}
+
+// The |k|^2 table of a geometry on the current device (cached).
+static int kk_table(const Derived &d, const float **out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    uint32_t bx, bz;
+    std::memcpy(&bx, &d.g.dx, 4);
+    std::memcpy(&bz, &d.g.dz, 4);
+    std::lock_guard<std::mutex> lk(g_mutex);
+    const auto key = std::make_tuple(dev, d.g.ntz, d.g.ntx, bx, bz);
+    auto it = g_kk_tables.find(key);
+    if (it != g_kk_tables.end()) {
+        *out = it->second;
+        return GB_FWI2D_OK;
+    }
+    float *t = nullptr;
+    const size_t bytes = sizeof(float) * d.kk.size();
+    if (cudaMalloc(&t, bytes) != cudaSuccess) return GB_FWI2D_ENOMEM;
+    if (cudaMemcpy(t, d.kk.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(t);
+        return GB_FWI2D_ECUDA;
+    }
+    g_kk_tables[key] = t;
+    *out = t;
+    return GB_FWI2D_OK;
+}
+
+// One pseudo-spectral time step of the wave's nres solves: pack p1, forward
+// transform, times -|k|^2, inverse transform, then the per-cell update and
+// the rest of the step.  Returns the number of this library's kernels.
+static int step_pstd(bool adj, const Geom &g, const Batch &b, int nres, const StepArgs &sa, cudaStream_t st)
+{
+    cufftHandle plan;
+    const CufftApi *api = cufft_api();
+    if (!api || fft_plan(g, nres, &plan) != GB_FWI2D_OK) {
+        t_enqueue_error = GB_FWI2D_ENOTSUP;
+        return 0;
+    }
+    const long long n = (long long)g.ntz * g.ntx;
+    const dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 1024), nres);
+    k_pstd_pack<<<grid, 256, 0, st>>>(g, b.ring, (sa.k + 1) % 3, b.spec);
+    cufftDoubleComplex *z = reinterpret_cast<cufftDoubleComplex *>(b.spec);
+    if (api->set_stream(plan, st) != CUFFT_SUCCESS || api->exec_z2z(plan, z, z, CUFFT_FORWARD) != CUFFT_SUCCESS)
+        t_enqueue_error = GB_FWI2D_ECUDA;
+    k_pstd_scale<<<grid, 256, 0, st>>>(n, b.kk, b.spec);
+    if (api->exec_z2z(plan, z, z, CUFFT_INVERSE) != CUFFT_SUCCESS) t_enqueue_error = GB_FWI2D_ECUDA;
+    const dim3 cells((unsigned)((n + 255) / 256), nres);
+    if (adj)
+        k_step_pstd<true><<<cells, 256, 0, st>>>(g, b, sa, b.spec);
+    else
+        k_step_pstd<false><<<cells, 256, 0, st>>>(g, b, sa, b.spec);
+    return 3;
+}
+
+// One time step of the wave; returns the number of this library's kernels.
+static int step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
+                cudaStream_t st)
+{
+    if (g.pstd) return step_pstd(adj, g, b, nres, sa, st);
     switch (g.Lc - 1) {
     case 3: launch_step<3>(adj, m, g, b, nres, sa, st); break;
     case 4: launch_step<4>(adj, m, g, b, nres, sa, st); break;
     case 5: launch_step<5>(adj, m, g, b, nres, sa, st); break;
     default: launch_step<6>(adj, m, g, b, nres, sa, st); break;
     }
+    return 1;
 }
 
 struct Call {
@@ -519,6 +663,7 @@ struct Call {
     bool profile;
     Maps maps;
     Maps maps2;  // checkpointing: the adjoint's ring
+    const float *kk = nullptr;  // pseudo-spectral mode: |k|^2 table on the device
 };
 
 static int grid_for(long long n, int threads)
@@ -577,8 +722,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
         sa.it = k;
         sa.snap = -1;
         sa.rik = c.d->rik[k];
-        step(false, c.maps, g, b, nres, sa, st);
-        ++launches;
+        launches += step(false, c.maps, g, b, nres, sa, st);
     }
     close_span(e0, e1, g.nt);
 
@@ -601,8 +745,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
             sa.it = k;
             sa.snap = (k % g.nti) == 0 ? k / g.nti - snap0 : -1;
             sa.rik = c.d->rik[k];
-            step(false, c.maps, g, b, nres, sa, st);
-            ++launches;
+            launches += step(false, c.maps, g, b, nres, sa, st);
         }
         for (int it = k1 - 1; it >= k0; --it) {  // the segment's adjoint steps
             StepArgs sa;
@@ -610,8 +753,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
             sa.it = it;
             sa.snap = (it % g.nti) == 0 ? it / g.nti - snap0 : -1;
             sa.rik = 0.0f;
-            step(true, c.maps2, g, ba, nres, sa, st);
-            ++launches;
+            launches += step(true, c.maps2, g, ba, nres, sa, st);
         }
     }
     close_span(e0, e1, 2LL * g.nt);
@@ -691,8 +833,7 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
         sa.it = it;
         sa.snap = -1;
         sa.rik = c.d->rik[it];
-        step(false, c.maps, g, b, nres, sa, st);
-        ++launches;
+        launches += step(false, c.maps, g, b, nres, sa, st);
     };
     auto level_out = [&](int it, int slot_level, int nres) {  // P^{it+1} -> store level
         cudaMemcpy2DAsync((char *)store + (size_t)slot_level * fbytes, store_pitch,
@@ -789,6 +930,8 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.imaging = imaging ? 1 : 0;
     b.store = fwd_only ? 0 : 1;
     b.status = status;
+    b.spec = (double2 *)(c.work + c.L.spec);
+    b.kk = c.kk;
     const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
@@ -815,8 +958,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
                 sa.it = adj ? g.nt - 1 - k : k;
                 sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
                 sa.rik = adj ? 0.0f : c.d->rik[sa.it];
-                step(adj, maps, g, b, nres, sa, st);
-                ++launches;
+                launches += step(adj, maps, g, b, nres, sa, st);
             }
             if (e1) {
                 cudaEventRecord(e1, st);
@@ -975,6 +1117,7 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     const bool ckpt = (flags & GB_FWI2D_CHECKPOINT) != 0;
     const bool exact = (flags & GB_FWI2D_EXACT_GRADIENT) != 0;
     if (exact && (flags & GB_FWI2D_IMAGING)) return GB_FWI2D_EINVAL;
+    if (exact && d.g.pstd && !(flags & GB_FWI2D_FORWARD_ONLY)) return GB_FWI2D_ENOTSUP;  // transposes the FD stencil
     Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0, ckpt, exact);
     if (work_bytes < L.total) return GB_FWI2D_ENOMEM;
     Call c;
@@ -996,14 +1139,26 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
         return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);
     if (st) return st;
+    if (d.g.pstd) {
+        // The transform plans exist before anything is enqueued: full waves,
+        // the last partial wave and single solves (GB_FWI2D_PLAIN).
+        st = kk_table(d, &c.kk);
+        if (st) return st;
+        const long long ninst = (long long)nsamples * d.g.ns;
+        cufftHandle h;
+        for (long long batch : {(long long)L.resident, ninst % L.resident, 1LL})
+            if (batch > 0 && (st = fft_plan(d.g, (int)batch, &h)) != GB_FWI2D_OK) return st;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     long long launches = 0;
-    if (flags & GB_FWI2D_GRAPH) {
+    t_enqueue_error = 0;
+    if ((flags & GB_FWI2D_GRAPH) && !d.g.pstd) {  // the transforms run eagerly, outside graphs
         st = run_graph(c, s, launches);
     } else {
         launches = enqueue(c, s);
         st = cudaGetLastError() == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
     }
+    if (st == GB_FWI2D_OK && t_enqueue_error) st = t_enqueue_error;
     t_last_launches = launches;
     return st;
 }
@@ -1041,6 +1196,7 @@ double gb_fwi2d_profile_step_ms(long long *launches)
 
 void gb_fwi2d_release_caches(void)
 {
+    const CufftApi *api = g_fft_plans.empty() ? nullptr : cufft_api();
     std::lock_guard<std::mutex> lk(g_mutex);
     for (auto &kv : g_graphs) cudaGraphExecDestroy(kv.second.exec);
     g_graphs.clear();
@@ -1048,6 +1204,11 @@ void gb_fwi2d_release_caches(void)
         cudaFree(kv.second.coef);
     }
     g_tables.clear();
+    if (api)
+        for (auto &kv : g_fft_plans) api->destroy(kv.second);
+    g_fft_plans.clear();
+    for (auto &kv : g_kk_tables) cudaFree(kv.second);
+    g_kk_tables.clear();
 }
 
 }  // extern "C"
@@ -1200,6 +1361,7 @@ extern "C" int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, co
     Derived d;
     int st = derive(*p, d);
     if (st) return st;
+    if (d.g.pstd) return GB_FWI2D_ENOTSUP;  // the transform library allocates its plans
     const bool fwd_only = (flags & GB_FWI2D_FORWARD_ONLY) != 0;
     const size_t coef_bytes = align256(sizeof(BlendCoef) * d.coef.size());
     const size_t cap = GB_FWI2D_STATIC_SCRATCH_BYTES;

@@ -90,6 +90,7 @@ struct Geom {
     int ns, nt, nti, nt_save;
     int tiles_x, tiles_z;
     int fast_dx, fast_dz, fast_dt;  // the host proved div_const exact for this divisor
+    int pstd;            // laplace_solver = 1: pseudo-spectral Laplacian
     long long fstride;   // floats per padded field (ntz * pitch)
     long long pstride;   // floats per interior snapshot (nz * ipitch)
     float dx, dz, dt;
@@ -112,6 +113,8 @@ struct Batch {
     int inst0;           // first solve of this wave
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
+    double2 *spec;       // pseudo-spectral mode: [resident][ntz][ntx] transform work array
+    const float *kk;     // pseudo-spectral mode: |k|^2 per padded cell (wavenumber)
 };
 
 // Per-launch step data.

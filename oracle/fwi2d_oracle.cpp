@@ -37,6 +37,7 @@
  */
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -89,7 +90,7 @@ int make_geometry(const oracle_params &p, Geometry &g)
     if (p.nx <= 0 || p.nz <= 0 || p.pml0 <= 0 || p.ns <= 0 || p.nt <= 0 || p.nr <= 0 ||
         p.nt_interval <= 0)
         return ORACLE_EINVAL;
-    if (p.laplace_solver != 0) return ORACLE_EINVAL; /* pseudo-spectral path is not restated */
+    if (p.laplace_solver != 0 && p.laplace_solver != 1) return ORACLE_EINVAL;
     if (p.Lc < 3 || p.Lc > 6) return ORACLE_EINVAL;  /* fd_coefficient knows Lc+1 = 4..7 */
     g.Lc = p.Lc + 1;
     g.pml = p.pml0 + g.Lc;
@@ -156,6 +157,53 @@ void ricker(int nt, Real dt, Real f0, Real *rik)
     }
 }
 
+/* wavenumber (fdtd2D_modelling.c:1127-1184): |k|^2 of the padded grid's DFT
+ * bins, kx = 2 pi dkx min(ix, ntx - ix) with the upper half starting at
+ * ceil(ntx/2), dkx = 1/ntx/dx stored as float, each |k| component stored as
+ * float, the squares summed in double and stored as float. */
+void wavenumber(int ntx, int ntz, float dx, float dz, std::vector<float> &k)
+{
+    const float dkz = (float)(1.0 / ntz / dz), dkx = (float)(1.0 / ntx / dx);
+    const int ax = ntx / 2 * 2 < ntx ? ntx / 2 + 1 : ntx / 2;
+    const int az = ntz / 2 * 2 < ntz ? ntz / 2 + 1 : ntz / 2;
+    k.assign((size_t)ntx * ntz, 0.0f);
+    for (int iz = 0; iz < ntz; ++iz)
+        for (int ix = 0; ix < ntx; ++ix) {
+            const float kz = (float)(2 * kPi * dkz * (iz < az ? iz : ntz - iz));
+            const float kx = (float)(2 * kPi * dkx * (ix < ax ? ix : ntx - ix));
+            k[(size_t)iz * ntx + ix] = (float)(std::pow((double)kx, 2.0) + std::pow((double)kz, 2.0));
+        }
+}
+
+/* Unnormalised 2-D DFT of a [ntz][ntx] complex array in place, sign -1
+ * (forward) or +1 (inverse) as FFTW_FORWARD / FFTW_BACKWARD: rows, then
+ * columns, each a direct O(n^2) sum with twiddles from one cos/sin table.
+ * The reference uses FFTW (absent here); any DFT agrees with it to double
+ * round-off. */
+void dft2(std::vector<std::complex<double>> &a, int ntz, int ntx, int sign)
+{
+    auto pass = [&](int n, int count, long long stride, long long step) {
+        std::vector<std::complex<double>> tw(n);
+        for (int j = 0; j < n; ++j) {
+            const double ang = 2.0 * 3.14159265358979323846 * j / n;
+            tw[j] = std::complex<double>(std::cos(ang), sign * std::sin(ang));
+        }
+#pragma omp parallel for schedule(static)
+        for (int line = 0; line < count; ++line) {
+            std::vector<std::complex<double>> in(n), out(n);
+            for (int j = 0; j < n; ++j) in[j] = a[line * step + j * stride];
+            for (int k = 0; k < n; ++k) {
+                std::complex<double> acc = 0.0;
+                for (int j = 0; j < n; ++j) acc += in[j] * tw[(long long)k * j % n];
+                out[k] = acc;
+            }
+            for (int j = 0; j < n; ++j) a[line * step + j * stride] = out[j];
+        }
+    };
+    pass(ntx, ntz, 1, ntx);  // along x for every row
+    pass(ntz, ntx, ntx, 1);  // along z for every column
+}
+
 inline float cube(float v) { return powf(v, 3); }
 inline double cube(double v) { return std::pow(v, 3); }
 
@@ -169,9 +217,15 @@ struct Engine {
     std::vector<Real> p0, p1, p2;
     std::vector<Real> psave; /* [nt_save][nz*nx], interior only */
     std::vector<Real> record;
+    std::vector<float> kk;                     /* pseudo-spectral |k|^2 */
+    std::vector<std::complex<double>> spec;    /* pseudo-spectral work array */
 
     Engine(const oracle_params &pp, const Geometry &gg) : p(pp), g(gg)
     {
+        if (p.laplace_solver == 1) {
+            wavenumber(g.ntx, g.ntz, p.dx, p.dz, kk);
+            spec.resize(g.ntp);
+        }
         dx = (Real)p.dx; dz = (Real)p.dz; dt = (Real)p.dt;
         fd_weights<Real>(g.Lc, fd);
         rik.resize(p.nt);
@@ -259,6 +313,33 @@ struct Engine {
 
     /* abc_for_p (fdtd2D_modelling.c:833-900): top, bottom, left, right, in
      * that order; the corner cells take two blends. */
+    /* pstd_2d_calculate_p (fdtd2D_modelling.c:783-830): p1 through a double
+     * 2-D DFT, times -|k|^2, back, and p2 = 2 p1 - p0 + (v dt)^2 re / (ntx ntz)
+     * over every cell, the float part evaluated in float and the sum in double
+     * as the C expression promotes it. */
+    void pstd()
+    {
+        const int ntp = g.ntp;
+        for (int i = 0; i < ntp; ++i) spec[i] = std::complex<double>((double)p1[i], 0.0);
+        dft2(spec, g.ntz, g.ntx, -1);
+        for (int i = 0; i < ntp; ++i) spec[i] *= -(double)kk[i];
+        dft2(spec, g.ntz, g.ntx, +1);
+        const double n = (double)g.ntx * g.ntz;
+        for (int i = 0; i < ntp; ++i) {
+            const Real a = 2 * p1[i] - p0[i];
+            p2[i] = (Real)((double)a + (double)vdt2[i] * spec[i].real() / n);
+        }
+    }
+
+    /* The Laplacian update of laplace_solver (forward_aco_2D :692-695). */
+    void laplacian()
+    {
+        if (p.laplace_solver == 1)
+            pstd();
+        else
+            stencil();
+    }
+
     void boundary()
     {
         const int Lc = g.Lc, pml = g.pml, ntx = g.ntx, ntz = g.ntz;
@@ -292,7 +373,7 @@ struct Engine {
         const int src = g.s_iz * ntx + g.s_ix[is];
         zero_fields();
         for (int it = 0; it < p.nt; ++it) {
-            stencil();
+            laplacian();
             boundary();
             p2[src] += rik[it] * dt * dt * velp[src] * velp[src];
             if (it % p.nt_interval == 0) {
@@ -315,7 +396,7 @@ struct Engine {
         const int ntx = g.ntx, pml = g.pml, nx = p.nx, nz = p.nz;
         zero_fields();
         for (int it = p.nt - 1; it >= 0; --it) {
-            stencil();
+            laplacian();
             boundary();
             for (int ir = 0; ir < p.nr; ++ir) {
                 const int c = g.r_iz * ntx + g.r_ix[ir];
@@ -608,6 +689,7 @@ int oracle_exact_grad_f64(const oracle_params *pp, const double *vel, const doub
     Geometry g;
     int st = make_geometry(*pp, g);
     if (st) return st;
+    if (pp->laplace_solver != 0) return ORACLE_EINVAL;  // the exact adjoint transposes the FD stencil
     Engine<double> e(*pp, g);
     e.pad_velocity(vel);
     ExactShot x(*pp, g, e);
@@ -623,6 +705,23 @@ int oracle_exact_grad_f64(const oracle_params *pp, const double *vel, const doub
             grad[jz * pp->nx + jx] += gpad[(size_t)iz * g.ntx + ix];
         }
     if (misfit) *misfit = J;
+    return ORACLE_OK;
+}
+
+/* The pseudo-spectral Laplacian of one [ntz][ntx] field (pstd_2d_calculate_p's
+ * DFT / -|k|^2 / inverse DFT part), out = re / (ntx ntz), for checks against
+ * known transforms. */
+int oracle_pstd_laplacian(int ntz, int ntx, float dx, float dz, const double *in, double *out)
+{
+    if (ntz <= 0 || ntx <= 0) return ORACLE_EINVAL;
+    std::vector<float> k;
+    wavenumber(ntx, ntz, dx, dz, k);
+    std::vector<std::complex<double>> a((size_t)ntz * ntx);
+    for (size_t i = 0; i < a.size(); ++i) a[i] = in[i];
+    dft2(a, ntz, ntx, -1);
+    for (size_t i = 0; i < a.size(); ++i) a[i] *= -(double)k[i];
+    dft2(a, ntz, ntx, +1);
+    for (size_t i = 0; i < a.size(); ++i) out[i] = a[i].real() / ((double)ntx * ntz);
     return ORACLE_OK;
 }
 

@@ -127,6 +127,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_forward2d_f32.argtypes = [P, fp32, fp32]
         L.oracle_forward2d_f64.argtypes = [P, fp64, fp64]
         L.oracle_exact_grad_f64.argtypes = [P, fp64, fp64, fp64, fp64]
+        L.oracle_pstd_laplacian.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, fp64, fp64]
         L.oracle_read_params.argtypes = [ctypes.c_char_p, P]
         L.oracle_ricker_f32.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float, fp32]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
@@ -227,6 +228,17 @@ def exact_grad_f64(p: Params, vel, obs):
     if st:
         raise ValueError(f"oracle_exact_grad_f64 status {st}")
     return J.value, grad
+
+
+def pstd_laplacian(field, dx: float, dz: float) -> np.ndarray:
+    """The pseudo-spectral Laplacian of a [ntz, ntx] field (float64)."""
+    f = np.ascontiguousarray(field, dtype=np.float64)
+    out = np.zeros_like(f)
+    st = lib().oracle_pstd_laplacian(f.shape[0], f.shape[1], float(dx), float(dz), _ptr(f, ctypes.c_double),
+                                     _ptr(out, ctypes.c_double))
+    if st:
+        raise ValueError(f"oracle_pstd_laplacian status {st}")
+    return out
 
 
 def misfit_f64(p: Params, vel, obs) -> float:

@@ -96,7 +96,8 @@ def _status(engine_lib, p):
 def test_validation_codes(engine_lib):
     good = cases.SMALL["fwi_o8"]["params"]
     assert _status(engine_lib, good) == _native.OK
-    assert _status(engine_lib, good.replace(laplace_solver=1)) == _native.ENOTSUP
+    assert _status(engine_lib, good.replace(laplace_solver=1)) == _native.OK      # pseudo-spectral
+    assert _status(engine_lib, good.replace(laplace_solver=2)) == _native.EINVAL
     assert _status(engine_lib, good.replace(Lc=7)) == _native.EINVAL
     assert _status(engine_lib, good.replace(nx=0)) == _native.EINVAL
     assert _status(engine_lib, good.replace(dr=0)) == _native.EINVAL          # 36 receivers in one cell
@@ -128,9 +129,23 @@ def test_batch_rejects_bad_arguments_without_gpu(engine_lib):
     cp = p.c()
     st = engine_lib.gb_fwi2d_batch(ctypes.byref(cp), 0, None, None, None, None, None, 0, 0, None, 0, None)
     assert st == _native.EINVAL
-    bad = p.replace(laplace_solver=1).c()
+    bad = p.replace(laplace_solver=2).c()
     st = engine_lib.gb_fwi2d_batch(ctypes.byref(bad), 1, 1, 1, None, None, None, 0, 0, 1, 1 << 30, None)
+    assert st == _native.EINVAL
+    # pseudo-spectral mode: no exact adjoint (it transposes the FD stencil), no static scratch
+    ps = p.replace(laplace_solver=1).c()
+    st = engine_lib.gb_fwi2d_batch(ctypes.byref(ps), 1, 1, 1, None, None, None, _native.FLAG_EXACT_GRADIENT, 0, 1,
+                                   1 << 30, None)
     assert st == _native.ENOTSUP
+    assert engine_lib.gb_fwi2d_batch_noalloc(ctypes.byref(ps), 1, 1, 1, None, None, None, 0, None) == _native.ENOTSUP
+
+
+def test_pseudo_spectral_workspace(engine_lib):
+    """laplace_solver = 1 adds one dense complex-double transform array per resident solve."""
+    p = cases.SMALL["fwi_o8"]["params"]
+    fd = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.c()), 2, 3, 0)
+    ps = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.replace(laplace_solver=1).c()), 2, 3, 0)
+    assert ps - fd >= 16 * p.ntp * 3
 
 
 def test_checkpoint_workspace_is_smaller(engine_lib):
