@@ -238,7 +238,7 @@ struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
     size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
     size_t store, lam, gpad;  // exact gradient only: forward levels, adjoint levels, padded dJ/dv
-    size_t spec;              // pseudo-spectral mode: [resident][ntz][ntx] complex double
+    size_t spec;              // pseudo-spectral mode: real field + half spectrum per resident solve
     int resident;
     int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
 };
@@ -315,7 +315,9 @@ static Layout plan_layout(const Geom &g, int nsamples, int resident, bool syn_in
     if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
     L.part = off;  off = align256(off + sizeof(double) * kMisfitBlocks * nsamples);
     L.spec = off;
-    if (g.pstd) off = align256(off + sizeof(double2) * (size_t)g.ntz * g.ntx * resident);
+    if (g.pstd)
+        off = align256(off + align256(sizeof(double) * (size_t)g.ntz * g.ntx * resident) +
+                       sizeof(double2) * (size_t)g.ntz * (g.ntx / 2 + 1) * resident);
     L.total = off;
     return L;
 }
@@ -529,7 +531,8 @@ static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, 
 struct CufftApi {
     decltype(&cufftPlanMany) plan_many = nullptr;
     decltype(&cufftSetStream) set_stream = nullptr;
-    decltype(&cufftExecZ2Z) exec_z2z = nullptr;
+    decltype(&cufftExecD2Z) exec_d2z = nullptr;
+    decltype(&cufftExecZ2D) exec_z2d = nullptr;
     decltype(&cufftDestroy) destroy = nullptr;
 };
 
@@ -546,27 +549,29 @@ static const CufftApi *cufft_api()
         if (h) {
             api.plan_many = (decltype(api.plan_many))dlsym(h, "cufftPlanMany");
             api.set_stream = (decltype(api.set_stream))dlsym(h, "cufftSetStream");
-            api.exec_z2z = (decltype(api.exec_z2z))dlsym(h, "cufftExecZ2Z");
+            api.exec_d2z = (decltype(api.exec_d2z))dlsym(h, "cufftExecD2Z");
+            api.exec_z2d = (decltype(api.exec_z2d))dlsym(h, "cufftExecZ2D");
             api.destroy = (decltype(api.destroy))dlsym(h, "cufftDestroy");
-            ok = api.plan_many && api.set_stream && api.exec_z2z && api.destroy;
+            ok = api.plan_many && api.set_stream && api.exec_d2z && api.exec_z2d && api.destroy;
         }
     }
     return ok ? &api : nullptr;
 }
 
-static std::map<std::tuple<int, int, int, int>, cufftHandle> g_fft_plans;  // (device, ntz, ntx, batch)
+static std::map<std::tuple<int, int, int, int, int>, cufftHandle> g_fft_plans;  // (device, ntz, ntx, batch, dir)
 static std::map<std::tuple<int, int, int, uint32_t, uint32_t>, float *> g_kk_tables;  // (device, ntz, ntx, dx, dz)
 static thread_local int t_enqueue_error = 0;
 
-// A batched in-place 2-D double-complex plan for `batch` dense [ntz][ntx] arrays.
-static int fft_plan(const Geom &g, int batch, cufftHandle *out)
+// Batched 2-D plans for `batch` fields: real [ntz][ntx] -> half spectrum
+// [ntz][ntx/2+1] (forward, D2Z) or back (inverse, Z2D), out of place.
+static int fft_plan(const Geom &g, int batch, bool inverse, cufftHandle *out)
 {
     const CufftApi *api = cufft_api();
     if (!api) return GB_FWI2D_ENOTSUP;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
     std::lock_guard<std::mutex> lk(g_mutex);
-    const auto key = std::make_tuple(dev, g.ntz, g.ntx, batch);
+    const auto key = std::make_tuple(dev, g.ntz, g.ntx, batch, inverse ? 1 : 0);
     auto it = g_fft_plans.find(key);
     if (it != g_fft_plans.end()) {
         *out = it->second;
@@ -574,9 +579,11 @@ static int fft_plan(const Geom &g, int batch, cufftHandle *out)
     }
     cufftHandle h;
     int n[2] = {g.ntz, g.ntx};
-    const int dist = g.ntz * g.ntx;
-    if (api->plan_many(&h, 2, n, nullptr, 1, dist, nullptr, 1, dist, CUFFT_Z2Z, batch) != CUFFT_SUCCESS)
-        return GB_FWI2D_ENOMEM;
+    int rn[2] = {g.ntz, g.ntx}, cn[2] = {g.ntz, g.ntx / 2 + 1};
+    const int rdist = g.ntz * g.ntx, cdist = g.ntz * (g.ntx / 2 + 1);
+    const cufftResult r = inverse ? api->plan_many(&h, 2, n, cn, 1, cdist, rn, 1, rdist, CUFFT_Z2D, batch)
+                                  : api->plan_many(&h, 2, n, rn, 1, rdist, cn, 1, cdist, CUFFT_D2Z, batch);
+    if (r != CUFFT_SUCCESS) return GB_FWI2D_ENOMEM;
     g_fft_plans[key] = h;
     *out = h;
     return GB_FWI2D_OK;
@@ -614,25 +621,28 @@ static int kk_table(const Derived &d, const float **out)
 // the rest of the step.  Returns the number of this library's kernels.
 static int step_pstd(bool adj, const Geom &g, const Batch &b, int nres, const StepArgs &sa, cudaStream_t st)
 {
-    cufftHandle plan;
+    cufftHandle fwd, inv;
     const CufftApi *api = cufft_api();
-    if (!api || fft_plan(g, nres, &plan) != GB_FWI2D_OK) {
+    if (!api || fft_plan(g, nres, false, &fwd) != GB_FWI2D_OK || fft_plan(g, nres, true, &inv) != GB_FWI2D_OK) {
         t_enqueue_error = GB_FWI2D_ENOTSUP;
         return 0;
     }
     const long long n = (long long)g.ntz * g.ntx;
+    double *real = b.spec;
+    cufftDoubleComplex *half = reinterpret_cast<cufftDoubleComplex *>(
+        (char *)b.spec + align256(sizeof(double) * (size_t)n * b.spec_resident));
     const dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 1024), nres);
-    k_pstd_pack<<<grid, 256, 0, st>>>(g, b.ring, (sa.k + 1) % 3, b.spec);
-    cufftDoubleComplex *z = reinterpret_cast<cufftDoubleComplex *>(b.spec);
-    if (api->set_stream(plan, st) != CUFFT_SUCCESS || api->exec_z2z(plan, z, z, CUFFT_FORWARD) != CUFFT_SUCCESS)
+    k_pstd_pack<<<grid, 256, 0, st>>>(g, b.ring, (sa.k + 1) % 3, real);
+    if (api->set_stream(fwd, st) != CUFFT_SUCCESS || api->exec_d2z(fwd, real, half) != CUFFT_SUCCESS)
         t_enqueue_error = GB_FWI2D_ECUDA;
-    k_pstd_scale<<<grid, 256, 0, st>>>(n, b.kk, b.spec);
-    if (api->exec_z2z(plan, z, z, CUFFT_INVERSE) != CUFFT_SUCCESS) t_enqueue_error = GB_FWI2D_ECUDA;
+    k_pstd_scale<<<grid, 256, 0, st>>>(g, b.kk, reinterpret_cast<double2 *>(half));
+    if (api->set_stream(inv, st) != CUFFT_SUCCESS || api->exec_z2d(inv, half, real) != CUFFT_SUCCESS)
+        t_enqueue_error = GB_FWI2D_ECUDA;
     const dim3 cells((unsigned)((n + 255) / 256), nres);
     if (adj)
-        k_step_pstd<true><<<cells, 256, 0, st>>>(g, b, sa, b.spec);
+        k_step_pstd<true><<<cells, 256, 0, st>>>(g, b, sa, real);
     else
-        k_step_pstd<false><<<cells, 256, 0, st>>>(g, b, sa, b.spec);
+        k_step_pstd<false><<<cells, 256, 0, st>>>(g, b, sa, real);
     return 3;
 }
 
@@ -930,7 +940,8 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.imaging = imaging ? 1 : 0;
     b.store = fwd_only ? 0 : 1;
     b.status = status;
-    b.spec = (double2 *)(c.work + c.L.spec);
+    b.spec = (double *)(c.work + c.L.spec);
+    b.spec_resident = c.L.resident;
     b.kk = c.kk;
     const Maps &maps = c.maps;
 
@@ -1147,7 +1158,8 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
         const long long ninst = (long long)nsamples * d.g.ns;
         cufftHandle h;
         for (long long batch : {(long long)L.resident, ninst % L.resident, 1LL})
-            if (batch > 0 && (st = fft_plan(d.g, (int)batch, &h)) != GB_FWI2D_OK) return st;
+            for (bool inverse : {false, true})
+                if (batch > 0 && (st = fft_plan(d.g, (int)batch, inverse, &h)) != GB_FWI2D_OK) return st;
     }
     cudaStream_t s = (cudaStream_t)stream;
     long long launches = 0;

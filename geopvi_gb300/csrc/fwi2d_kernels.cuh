@@ -113,8 +113,11 @@ struct Batch {
     int inst0;           // first solve of this wave
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
-    double2 *spec;       // pseudo-spectral mode: [resident][ntz][ntx] transform work array
+    double *spec;        // pseudo-spectral mode: [resident][ntz][ntx] real array, then the
+                         // [resident][ntz][ntx/2+1] half spectrum right after it
     const float *kk;     // pseudo-spectral mode: |k|^2 per padded cell (wavenumber)
+    int spec_resident;   // pseudo-spectral mode: solves the real array holds (the half
+                         // spectrum starts after them)
 };
 
 // Per-launch step data.

@@ -10,39 +10,46 @@
 // the FD mode (forward_aco_2D :692-700, backward_aco_2D :732-740).
 //
 // On the GPU: k_pstd_pack copies p1 of every resident solve into a dense
-// [resident][ntz][ntx] complex double array, batched cuFFT Z2Z transforms
-// run in place around k_pstd_scale (times -|k|^2, the wavenumber table of
-// wavenumber() :1127-1184), and k_step_pstd applies the update and the rest
-// of the step per cell.  The transforms dominate; they run on the FP64
-// units, as the reference's FFTW does in double.
+// [resident][ntz][ntx] real double array; a batched cuFFT D2Z transform
+// gives the half spectrum [ntz][ntx/2 + 1] (the input is real, so the
+// reference's complex transform's other half is its mirror image and the
+// imaginary part of the result is zero); k_pstd_scale multiplies by -|k|^2
+// (the wavenumber table of wavenumber() :1127-1184, symmetric under
+// k -> -k); a Z2D transform returns the real part; k_step_pstd applies the
+// update and the rest of the step per cell.  The transforms dominate; they
+// run on the FP64 units, as the reference's FFTW does in double.
 #pragma once
 
 #include "fwi2d_kernels.cuh"
 
 namespace gbfwi {
 
-// spec[slot][iz][ix] = (p1, 0) for the wave's resident solves.
-__global__ void k_pstd_pack(const Geom g, const float *__restrict__ ring, int b1, double2 *__restrict__ spec)
+// real[slot][iz][ix] = p1 for the wave's resident solves.
+__global__ void k_pstd_pack(const Geom g, const float *__restrict__ ring, int b1, double *__restrict__ real)
 {
     const int slot = blockIdx.y;
     const long long n = (long long)g.ntz * g.ntx;
     const float *p1 = ring + ((long long)slot * 3 + b1) * g.fstride;
-    double2 *out = spec + (long long)slot * n;
+    double *out = real + (long long)slot * n;
     for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
          d += (long long)gridDim.x * blockDim.x) {
         const int iz = (int)(d / g.ntx), ix = (int)(d - (long long)iz * g.ntx);
-        out[d] = make_double2((double)p1[(long long)iz * g.pitch + ix + g.xoff], 0.0);
+        out[d] = (double)p1[(long long)iz * g.pitch + ix + g.xoff];
     }
 }
 
-// spec *= -k (k float, the product in double: indata = -k[..] * indata).
-__global__ void k_pstd_scale(long long n, const float *__restrict__ kk, double2 *__restrict__ spec)
+// half[slot][iz][jx] *= -k[iz][jx], jx <= ntx/2 (k float, the product in
+// double: indata = -k[..] * indata).
+__global__ void k_pstd_scale(const Geom g, const float *__restrict__ kk, double2 *__restrict__ half)
 {
     const int slot = blockIdx.y;
-    double2 *s = spec + (long long)slot * n;
+    const int nh = g.ntx / 2 + 1;
+    const long long n = (long long)g.ntz * nh;
+    double2 *s = half + (long long)slot * n;
     for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
          d += (long long)gridDim.x * blockDim.x) {
-        const double mk = -(double)kk[d];
+        const int iz = (int)(d / nh), jx = (int)(d - (long long)iz * nh);
+        const double mk = -(double)kk[(long long)iz * g.ntx + jx];
         const double2 v = s[d];
         s[d] = make_double2(__dmul_rn(mk, v.x), __dmul_rn(mk, v.y));
     }
@@ -55,7 +62,7 @@ __global__ void k_pstd_scale(long long n, const float *__restrict__ kk, double2 
 // the FD kernel's general sweep does them.
 template <bool ADJ>
 __global__ void __launch_bounds__(256) k_step_pstd(const Geom g, const Batch b, const StepArgs sa,
-                                                   const double2 *__restrict__ spec)
+                                                   const double *__restrict__ real)
 {
     const int slot = blockIdx.y;
     const int inst = b.inst0 + slot;
@@ -73,7 +80,7 @@ __global__ void __launch_bounds__(256) k_step_pstd(const Geom g, const Batch b, 
     const float p1c = p1[c], p0c = p0[c], vd = vdt[c];
 
     // 2*p1 - p0 + powf(v*dt, 2) * re / (ntx*ntz)
-    const double re = spec[(long long)slot * n + d].x;
+    const double re = real[(long long)slot * n + d];
     const double lap = __ddiv_rn(__dmul_rn((double)fm(vd, vd), re), (double)(g.ntx * g.ntz));
     float q = __double2float_rn(__dadd_rn((double)fs(fm(2.0f, p1c), p0c), lap));
 

@@ -1,11 +1,14 @@
 """GPU pseudo-spectral mode (laplace_solver = 1) against the oracle.
 
-The engine transforms with cuFFT (double), the oracle with a direct DFT
-(double); both round the same double Laplacian to float, so the data agree
-to float round-off rather than bit for bit.  Bars: synthetic data relative
-L2 <= 1e-5, gradient <= 1e-4 (the tolerances stated for this path), misfit
-<= 1e-5.  Parity with the reference itself is unpinned (its FFTW path cannot
-be built here).
+The engine transforms with cuFFT (double, real-to-complex), the oracle with
+a direct DFT (double); both round the double Laplacian to float every step,
+so the data agree to the scheme's round-off spread rather than bit for bit.
+That spread is intrinsic: two oracle builds differing only in the DFT's
+summation order (plain vs compensated) differ by 2.7-4.4e-6 on these cases,
+the FP32 and FP64 schemes by 3-5e-6, and the engine lands 1.9-8.2e-6 from
+the oracle.  Bars: synthetic data relative L2 <= 1e-5, gradient <= 1e-4
+(the tolerances stated for this path), misfit <= 1e-5.  Parity with the
+reference itself is unpinned (its FFTW path cannot be built here).
 """
 import os
 
