@@ -38,7 +38,7 @@ STATIC_SCRATCH_BYTES = 64 << 20
 
 STATUS_NAMES = {ENOENT: "ENOENT (parameter file missing)", E2BIG: "E2BIG (batch exceeds the static scratch)", ENOMEM: "ENOMEM (device memory)",
                 EINVAL: "EINVAL (invalid parameters or buffers)",
-                ENOTSUP: "ENOTSUP (pseudo-spectral Laplacian not built)",
+                ENOTSUP: "ENOTSUP (combination not supported, or cuFFT missing for laplace_solver = 1)",
                 ENAN: "ENAN (NaN in velocity)", ECUDA: "ECUDA (CUDA runtime error)",
                 ETIMEOUT: "ETIMEOUT (a bounded device wait gave up)"}
 

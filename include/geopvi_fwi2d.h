@@ -35,7 +35,9 @@ extern "C" {
 #define GB_FWI2D_E2BIG (-7)      /* batch needs more than the static scratch (gb_fwi2d_batch_noalloc) */
 #define GB_FWI2D_ENOMEM (-12)    /* device memory / workspace too small */
 #define GB_FWI2D_EINVAL (-22)    /* bad geometry, sizes or pointers */
-#define GB_FWI2D_ENOTSUP (-95)   /* valid in the reference but not built here */
+#define GB_FWI2D_ENOTSUP (-95)   /* a combination this library does not run (the exact gradient or the
+                                    allocation-free entry with laplace_solver = 1), or the FFT
+                                    library the pseudo-spectral mode loads is missing */
 #define GB_FWI2D_ENAN (-1001)    /* NaN/Inf in the velocity input */
 #define GB_FWI2D_ECUDA (-1002)   /* a CUDA runtime call failed */
 #define GB_FWI2D_ETIMEOUT (-1003) /* a bounded device wait gave up (status word set) */
@@ -69,7 +71,9 @@ typedef struct gb_fwi2d_params {
 int gb_fwi2d_read_params(const char *path, gb_fwi2d_params *out);
 
 /* Check a parameter set the way the solver needs it (grid, geometry inside
- * the padded grid, FD order, time sampling).  GB_FWI2D_OK or EINVAL/ENOTSUP. */
+ * the padded grid, FD order, time sampling).  GB_FWI2D_OK or EINVAL.  laplace_solver 0
+ * selects the FD stencil, 1 the pseudo-spectral Laplacian (double 2-D transforms through
+ * cuFFT, loaded on first use). */
 int gb_fwi2d_validate(const gb_fwi2d_params *p);
 
 /* Drop-in for fwi_2D (fdtd2D_modelling.c:18-353, bound at pyacofwi2D.pyx:4).
