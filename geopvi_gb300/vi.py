@@ -380,3 +380,14 @@ def psvi_mask_2D(correlation, ndim, nx=1, nz=1):
             mask[i, -off:] = False
             i += 1
     return mask
+
+
+def get_flow_param(flow):
+    """[u, exp(diag), off-diagonals] of a Linear flow: the layout ``Linear(param=...)``
+    reads, saved after one frequency band to start the next
+    (examples/fwi3d/fwi3d.py:46-53 in the reference)."""
+    mus = flow.u.detach().cpu().numpy()
+    sigmas = np.exp(flow.diag.detach().cpu().numpy())
+    if flow.non_diag is None:
+        return np.hstack([mus, sigmas])
+    return np.hstack([mus, sigmas, flow.non_diag.detach().cpu().numpy().ravel()])

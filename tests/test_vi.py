@@ -102,6 +102,30 @@ def test_vi_update_reproduces_reference_iterations(g):
     assert close(q.flows[0].u, g["vi_u"], 1e-10) and close(q.flows[0].diag, g["vi_diag"], 1e-10)
 
 
+def test_flow_param_round_trip(g):
+    """get_flow_param -> Linear(param=...) starts the next frequency band from the last."""
+    dim = g["x"].shape[1]
+    x = torch.from_numpy(g["x"])
+    for kw in (dict(kernel="diagonal", param=g["diag_param"]), dict(kernel="fullrank", param=g["full_param"]),
+               dict(kernel="structured", mask=g["psvi_mask"], param=g["psvi_param"])):
+        f = vi.Linear(dim, **kw)
+        f2 = vi.Linear(dim, **{**kw, "param": vi.get_flow_param(f)})
+        assert torch.allclose(f(x)[0], f2(x)[0], rtol=1e-14, atol=0)
+
+
+@pytest.mark.gpu
+def test_waveform_generation(engine_lib, cuda, tmp_path):
+    """generate_waveform: the reference's (ns, nt, nr) float32 waveform.npy, bit-exact data."""
+    from geopvi_gb300.data import generate_waveform
+    z = np.load(os.path.join(os.path.dirname(cases.__file__), "fwi_o8.npz"))
+    p = cases.params_from_npz(z)
+    path = str(tmp_path / "waveform.npy")
+    data = generate_waveform(p, z["truth"].astype(np.float64), path=path, device=cuda)
+    back = np.load(path)
+    assert back.dtype == np.float32 and back.shape == (p.ns, p.nt, p.nr)
+    assert np.array_equal(back.ravel(), z["obs"]) and np.array_equal(data, back)
+
+
 @pytest.mark.gpu
 def test_vi_iteration_on_the_device(engine_lib, cuda, tmp_path):
     """A PSVI iteration of a small FWI posterior: every tensor of the step
