@@ -40,7 +40,7 @@ class Fwi2dEngine:
     """One solver configuration bound to one CUDA device.
 
     max_resident: (sample, shot) solves whose wavefield state is held at once;
-        None sizes it from ``hbm_budget`` (bytes, default 60% of free memory).
+        None sizes it from ``hbm_budget`` (bytes, default 80% of free memory), in waves of equal size.
     graph: capture the step sequence in a CUDA graph on first use and replay.
     plain: one solve per launch, shots in order -- the comparator form.
     checkpoint: keep the forward state every ~sqrt(nt) steps and recompute
@@ -85,11 +85,14 @@ class Fwi2dEngine:
         budget = self.hbm_budget
         if budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)
-            budget = int(free * 0.6)
+            budget = int(free * 0.8)
         base = self.workspace_bytes(nsamples, 1, flags)
         per = max(1, self.workspace_bytes(nsamples, 2, flags) - base) if ninst > 1 else 1
-        fit = 1 + max(0, (budget - base) // per)
-        return int(max(1, min(ninst, fit)))
+        fit = int(max(1, min(ninst, 1 + max(0, (budget - base) // per))))
+        # Equal waves: as many as the budget needs, each as full as the others
+        # (a short last wave would run a launch's worth of steps half empty).
+        waves = -(-ninst // fit)
+        return -(-ninst // waves)
 
     def _workspace(self, nsamples: int, flags: int) -> tuple[torch.Tensor, int]:
         """One workspace is held at a time; it is sized once per batch shape
