@@ -284,6 +284,7 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     step_ms, step_launches = eng.step_profile()
     device_status = eng.status()
+    step_variant = eng.tuned_variant(nsamples)  # -1: the tuner was still trying variants
     t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -377,6 +378,7 @@ def run_gpu(args):
                        "samples": nsamples, "shots": p.ns,
                        "grid": f"{p.nz}x{p.nx} (padded {p.ntz}x{p.ntx})", "nt": p.nt, "fd_order": 2 * p.Lc,
                        "resident_solves": resident, "waves": -(-ninst // resident),
+                       "fd_step_variant": step_variant,
                        "l2": "inputs larger than L2 (wavefield state of the resident solves >> 129 MB)",
                        "parallelism": f"replicas x{world}"},
             "sample_gradients_per_s": sgrad,

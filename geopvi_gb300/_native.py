@@ -33,6 +33,13 @@ FLAG_CHECKPOINT = 0x8
 FLAG_FORWARD_ONLY = 0x10
 FLAG_PROFILE = 0x20
 FLAG_EXACT_GRADIENT = 0x40
+VARIANT_SHIFT = 8
+NUM_STEP_VARIANTS = 4
+
+
+def flag_variant(v: int) -> int:
+    """Force FD step variant v (0-3); 0 in the flags lets the tuner choose."""
+    return (v + 1) << VARIANT_SHIFT
 
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -47,7 +54,7 @@ EXPORTED_SYMBOLS = (
     "gb_fwi2d_read_params", "gb_fwi2d_validate", "fwi_2D", "forward_2D",
     "gb_fwi2d_workspace_bytes", "gb_fwi2d_batch", "gb_fwi2d_last_launch_count",
     "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms", "gb_fwi2d_status",
-    "gb_fwi2d_batch_noalloc",
+    "gb_fwi2d_batch_noalloc", "gb_fwi2d_tuned_variant",
 )
 
 
@@ -104,6 +111,8 @@ def load() -> ctypes.CDLL:
         L.gb_fwi2d_profile_step_ms.restype = ctypes.c_double
         L.gb_fwi2d_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gb_fwi2d_status.restype = ctypes.c_int
+        L.gb_fwi2d_tuned_variant.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_uint]
+        L.gb_fwi2d_tuned_variant.restype = ctypes.c_int
         L.gb_fwi2d_release_caches.argtypes = []
         L.gb_fwi2d_release_caches.restype = None
         L.gb_fwi2d_version.argtypes = []

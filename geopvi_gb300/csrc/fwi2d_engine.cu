@@ -512,16 +512,29 @@ static bool make_maps(Maps &m, const Geom &g, float *ring, int resident)
     return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * (g.Lc - 1));
 }
 
-template <int H>
-static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
-                        const StepArgs &sa, cudaStream_t st)
+template <int H, int U, int MINB>
+static void launch_step_variant(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
+                                const StepArgs &sa, cudaStream_t st)
 {
     const dim3 grid(g.tiles_x * g.tiles_z, nres), block(kThreads);
     const int smem = TileShape<H>::kSmem;
     if (adj)
-        k_step<H, true><<<grid, block, smem, st>>>(m.p1, g, b, sa);
+        k_step<H, true, U, MINB><<<grid, block, smem, st>>>(m.p1, g, b, sa);
     else
-        k_step<H, false><<<grid, block, smem, st>>>(m.p1, g, b, sa);
+        k_step<H, false, U, MINB><<<grid, block, smem, st>>>(m.p1, g, b, sa);
+}
+
+template <int H>
+static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
+                        const StepArgs &sa, cudaStream_t st, int variant)
+{
+    static_assert(kNumStepVariants == 4, "one case per entry of kStepVariants");
+    switch (variant) {
+    case 1: launch_step_variant<H, kStepVariants[1].rows, kStepVariants[1].min_blocks>(adj, m, g, b, nres, sa, st); break;
+    case 2: launch_step_variant<H, kStepVariants[2].rows, kStepVariants[2].min_blocks>(adj, m, g, b, nres, sa, st); break;
+    case 3: launch_step_variant<H, kStepVariants[3].rows, kStepVariants[3].min_blocks>(adj, m, g, b, nres, sa, st); break;
+    default: launch_step_variant<H, kStepVariants[0].rows, kStepVariants[0].min_blocks>(adj, m, g, b, nres, sa, st); break;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -648,14 +661,14 @@ static int step_pstd(bool adj, const Geom &g, const Batch &b, int nres, const St
 
 // One time step of the wave; returns the number of this library's kernels.
 static int step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
-                cudaStream_t st)
+                cudaStream_t st, int variant)
 {
     if (g.pstd) return step_pstd(adj, g, b, nres, sa, st);
     switch (g.Lc - 1) {
-    case 3: launch_step<3>(adj, m, g, b, nres, sa, st); break;
-    case 4: launch_step<4>(adj, m, g, b, nres, sa, st); break;
-    case 5: launch_step<5>(adj, m, g, b, nres, sa, st); break;
-    default: launch_step<6>(adj, m, g, b, nres, sa, st); break;
+    case 3: launch_step<3>(adj, m, g, b, nres, sa, st, variant); break;
+    case 4: launch_step<4>(adj, m, g, b, nres, sa, st, variant); break;
+    case 5: launch_step<5>(adj, m, g, b, nres, sa, st, variant); break;
+    default: launch_step<6>(adj, m, g, b, nres, sa, st, variant); break;
     }
     return 1;
 }
@@ -674,6 +687,12 @@ struct Call {
     Maps maps;
     Maps maps2;  // checkpointing: the adjoint's ring
     const float *kk = nullptr;  // pseudo-spectral mode: |k|^2 table on the device
+    int variant = 0;            // k_step variant (kStepVariants)
+    // Tuning: waves [0, trials.size()) run variant trials[i] between events
+    // trial_ev[i]; later waves run `variant`.
+    std::vector<int> trials;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> trial_ev;
+    int wave_variant(long long wave) const { return wave < (long long)trials.size() ? trials[wave] : variant; }
 };
 
 static int grid_for(long long n, int threads)
@@ -732,7 +751,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
         sa.it = k;
         sa.snap = -1;
         sa.rik = c.d->rik[k];
-        launches += step(false, c.maps, g, b, nres, sa, st);
+        launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
     }
     close_span(e0, e1, g.nt);
 
@@ -755,7 +774,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
             sa.it = k;
             sa.snap = (k % g.nti) == 0 ? k / g.nti - snap0 : -1;
             sa.rik = c.d->rik[k];
-            launches += step(false, c.maps, g, b, nres, sa, st);
+            launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
         }
         for (int it = k1 - 1; it >= k0; --it) {  // the segment's adjoint steps
             StepArgs sa;
@@ -763,7 +782,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
             sa.it = it;
             sa.snap = (it % g.nti) == 0 ? it / g.nti - snap0 : -1;
             sa.rik = 0.0f;
-            launches += step(true, c.maps2, g, ba, nres, sa, st);
+            launches += step(true, c.maps2, g, ba, nres, sa, st, c.variant);
         }
     }
     close_span(e0, e1, 2LL * g.nt);
@@ -843,7 +862,7 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
         sa.it = it;
         sa.snap = -1;
         sa.rik = c.d->rik[it];
-        launches += step(false, c.maps, g, b, nres, sa, st);
+        launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
     };
     auto level_out = [&](int it, int slot_level, int nres) {  // P^{it+1} -> store level
         cudaMemcpy2DAsync((char *)store + (size_t)slot_level * fbytes, store_pitch,
@@ -950,11 +969,19 @@ static long long enqueue(const Call &c, cudaStream_t st)
     for (long long i0 = 0; i0 < ninst && ckpt; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
         b.inst0 = (int)i0;
-        launches += enqueue_checkpointed(c, b, nres, st);
+        const long long wi = i0 / wave;
+        Call cw = c;
+        cw.variant = c.wave_variant(wi);
+        if (wi < (long long)c.trials.size()) cudaEventRecord(c.trial_ev[wi].first, st);
+        launches += enqueue_checkpointed(cw, b, nres, st);
+        if (wi < (long long)c.trials.size()) cudaEventRecord(c.trial_ev[wi].second, st);
     }
     for (long long i0 = 0; i0 < ninst && !ckpt; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
         b.inst0 = (int)i0;
+        const long long wi = i0 / wave;
+        const int variant = c.wave_variant(wi);
+        if (wi < (long long)c.trials.size()) cudaEventRecord(c.trial_ev[wi].first, st);
         for (int pass = 0; pass < (fwd_only ? 1 : 2); ++pass) {
             const bool adj = pass == 1;
             // p0 and p1 of step 0 start at zero (wavefield_initialization).
@@ -969,7 +996,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
                 sa.it = adj ? g.nt - 1 - k : k;
                 sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
                 sa.rik = adj ? 0.0f : c.d->rik[sa.it];
-                launches += step(adj, maps, g, b, nres, sa, st);
+                launches += step(adj, maps, g, b, nres, sa, st, variant);
             }
             if (e1) {
                 cudaEventRecord(e1, st);
@@ -977,6 +1004,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
                 t_profile.launches += g.nt;
             }
         }
+        if (wi < (long long)c.trials.size()) cudaEventRecord(c.trial_ev[wi].second, st);
     }
     if (c.grad && !fwd_only) {
         k_reduce_grad<<<grid_for((long long)c.nsamples * g.nz * g.nx, 256), 256, 0, st>>>(
@@ -1008,6 +1036,7 @@ static std::vector<long long> graph_key(const Call &c, int dev)
     k.push_back((long long)(uintptr_t)c.work);
     k.push_back(c.flags);
     k.push_back(c.L.resident);
+    k.push_back(c.variant);
     // The Ricker table depends on f0, which Geom does not hold.
     for (float r : {c.d->rik.empty() ? 0.0f : c.d->rik[0], c.d->rik.size() > 1 ? c.d->rik[1] : 0.0f}) {
         int bits;
@@ -1015,6 +1044,79 @@ static std::vector<long long> graph_key(const Call &c, int dev)
         k.push_back(bits);
     }
     return k;
+}
+
+// ---------------------------------------------------------------------------
+// Variant tuner.  Every k_step variant computes the same values bit for bit,
+// so the caller's own work serves as trials: while a (geometry, batch size,
+// wave size, mode) has untried variants, each wave of a call runs one of them
+// between two events (a six-wave batch tries all four in its first call);
+// later calls read the finished timings -- polled, never waited for -- and
+// run the fastest.  Calls with trials run eagerly; graph capture starts once
+// the choice is made.
+// ---------------------------------------------------------------------------
+struct TuneState {
+    bool measured[kNumStepVariants] = {};
+    bool inflight[kNumStepVariants] = {};
+    float ms[kNumStepVariants] = {};
+    cudaEvent_t e0[kNumStepVariants] = {}, e1[kNumStepVariants] = {};
+    int best = 0;  // fastest measured (the default until one is measured)
+    bool done = false;
+};
+static std::mutex g_tune_mutex;
+static std::map<std::vector<long long>, TuneState> g_tune;
+
+static std::vector<long long> tune_key(const Geom &g, int nsamples, int resident, unsigned flags, int dev)
+{
+    std::vector<long long> k{dev, nsamples, resident,
+                             (long long)(flags & (GB_FWI2D_IMAGING | GB_FWI2D_PLAIN | GB_FWI2D_CHECKPOINT |
+                                                  GB_FWI2D_FORWARD_ONLY | GB_FWI2D_EXACT_GRADIENT))};
+    const int *gi = (const int *)&g;
+    for (size_t i = 0; i < sizeof(Geom) / sizeof(int); ++i) k.push_back(gi[i]);
+    return k;
+}
+
+// Read the trials whose events have completed (g_tune_mutex held).
+static void tune_harvest(TuneState &t)
+{
+    bool all = true;
+    for (int v = 0; v < kNumStepVariants; ++v) {
+        if (t.inflight[v] && cudaEventQuery(t.e1[v]) == cudaSuccess) {
+            float ms = 0.0f;
+            // An unreadable timing counts as measured and never wins.
+            t.ms[v] = cudaEventElapsedTime(&ms, t.e0[v], t.e1[v]) == cudaSuccess ? ms : 3.4e38f;
+            t.measured[v] = true;
+            t.inflight[v] = false;
+        }
+        all = all && t.measured[v];
+    }
+    int best = -1;
+    for (int v = 0; v < kNumStepVariants; ++v)
+        if (t.measured[v] && (best < 0 || t.ms[v] < t.ms[best])) best = v;
+    if (best >= 0) t.best = best;
+    t.done = all;
+}
+
+// The calling batch's plan: trial variants for its first waves (with their
+// events) and the variant for the rest.
+static void tune_plan(const std::vector<long long> &key, long long nwaves, Call &c)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    TuneState &t = g_tune[key];
+    tune_harvest(t);
+    c.variant = t.best;
+    if (t.done) return;
+    for (int v = 0; v < kNumStepVariants && (long long)c.trials.size() < nwaves; ++v) {
+        if (t.measured[v] || t.inflight[v]) continue;
+        if (!t.e0[v] && (cudaEventCreate(&t.e0[v]) != cudaSuccess || cudaEventCreate(&t.e1[v]) != cudaSuccess)) {
+            t.measured[v] = true;  // no events: leave this variant out
+            t.ms[v] = 3.4e38f;
+            continue;
+        }
+        t.inflight[v] = true;
+        c.trials.push_back(v);
+        c.trial_ev.emplace_back(t.e0[v], t.e1[v]);
+    }
 }
 
 static int run_graph(const Call &c, cudaStream_t st, long long &launches)
@@ -1164,7 +1266,20 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     cudaStream_t s = (cudaStream_t)stream;
     long long launches = 0;
     t_enqueue_error = 0;
-    if ((flags & GB_FWI2D_GRAPH) && !d.g.pstd) {  // the transforms run eagerly, outside graphs
+    // Kernel variant: forced by the flags, or planned by the tuner (FD mode;
+    // the exact gradient runs the tuned or default variant without trials).
+    const unsigned forced = (flags >> GB_FWI2D_VARIANT_SHIFT) & 0xFu;
+    if (forced > (unsigned)kNumStepVariants) return GB_FWI2D_EINVAL;
+    if (forced) {
+        c.variant = (int)forced - 1;
+    } else if (!d.g.pstd) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+        const long long wave = (flags & GB_FWI2D_PLAIN) ? 1 : L.resident;
+        const long long ninst = (long long)nsamples * d.g.ns;
+        tune_plan(tune_key(d.g, nsamples, L.resident, flags, dev), exact ? 0 : (ninst + wave - 1) / wave, c);
+    }
+    if ((flags & GB_FWI2D_GRAPH) && !d.g.pstd && c.trials.empty()) {  // transforms and trials run eagerly
         st = run_graph(c, s, launches);
     } else {
         launches = enqueue(c, s);
@@ -1176,6 +1291,23 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
 }
 
 long long gb_fwi2d_last_launch_count(void) { return t_last_launches; }
+
+int gb_fwi2d_tuned_variant(const gb_fwi2d_params *p, int nsamples, int max_resident, unsigned flags)
+{
+    if (!p || nsamples <= 0) return GB_FWI2D_EINVAL;
+    Derived d;
+    int st = derive(*p, d);
+    if (st) return st;
+    const Layout L = plan_layout(d.g, nsamples, max_resident, true, (flags & GB_FWI2D_FORWARD_ONLY) != 0,
+                                 (flags & GB_FWI2D_CHECKPOINT) != 0, (flags & GB_FWI2D_EXACT_GRADIENT) != 0);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GB_FWI2D_ECUDA;
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tune.find(tune_key(d.g, nsamples, L.resident, flags, dev));
+    if (it == g_tune.end()) return -1;
+    tune_harvest(it->second);
+    return it->second.done ? it->second.best : -1;
+}
 
 int gb_fwi2d_status(const void *work, void *stream)
 {

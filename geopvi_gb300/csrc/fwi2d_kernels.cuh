@@ -41,12 +41,18 @@ constexpr int kThreads = kTileX * kWarps;   // 128
 
 // Resident blocks per SM the step kernel is compiled for (register cap
 // 65536 / (128 * this)); a build-time tuning knob.
-// Rows per block of the interior sweep (loads run one block ahead).  Two
-// measured faster than four: the unrolled row bodies, each with its inline
-// exact fallbacks, otherwise overflow the instruction cache.
-#ifndef GB_FWI2D_ROWS_U
-#define GB_FWI2D_ROWS_U 2
-#endif
+// Kernel variants: rows per block of the interior sweep (U; loads run one
+// block ahead) and resident blocks per SM the registers are capped for.  All
+// variants compute the same values bit for bit; the engine's tuner times them
+// on the caller's own batches and keeps the fastest per geometry and batch
+// shape.  (2, 8) is the default: on the cfg2 grid four rows overflow the
+// instruction cache (the unrolled row bodies carry inline exact fallbacks)
+// and fewer blocks per SM lose latency hiding.
+struct StepVariant {
+    int rows, min_blocks;
+};
+constexpr StepVariant kStepVariants[] = {{2, 8}, {4, 8}, {1, 8}, {2, 6}};
+constexpr int kNumStepVariants = sizeof(kStepVariants) / sizeof(kStepVariants[0]);
 
 #ifndef GB_FWI2D_MIN_BLOCKS
 #define GB_FWI2D_MIN_BLOCKS 8
@@ -312,14 +318,13 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
 // Interior sweep: every cell of the warp is inside the interior of the
 // padded grid, away from the absorbing strips, the source and the receivers,
 // so each row is lean_row without per-cell region tests.  Rows go in blocks
-// of U = GB_FWI2D_ROWS_U: the z window covers the block (2H + U values), the
+// of U (a variant parameter): the z window covers the block (2H + U values), the
 // block's p0 / v*dt rows are fetched one block ahead, and the rows'
 // independent dependency chains interleave.
-template <int H, bool ADJ>
+template <int H, bool ADJ, int U>
 __device__ __forceinline__ void sweep_interior(const Geom &g, const Batch &b, const StepArgs &sa, const WarpCtx &w,
                                                float p0_first, float vd_first)
 {
-    constexpr int U = GB_FWI2D_ROWS_U;
     static_assert(kWarpRows % U == 0, "row blocks must tile the warp's rows");
     float win[2 * H + U];
 #pragma unroll
@@ -500,8 +505,8 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
 // per block.  Each warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
-template <int H, bool ADJ>
-__global__ void __launch_bounds__(kThreads, GB_FWI2D_MIN_BLOCKS)
+template <int H, bool ADJ, int U = 2, int MINB = GB_FWI2D_MIN_BLOCKS>
+__global__ void __launch_bounds__(kThreads, MINB)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
     using TS = TileShape<H>;
@@ -577,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, GB_FWI2D_MIN_BLOCKS)
                           (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
                           (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
     if (interior)
-        sweep_interior<H, ADJ>(g, b, sa, w, p0_next, vd_next);
+        sweep_interior<H, ADJ, U>(g, b, sa, w, p0_next, vd_next);
     else
         sweep_general<H, ADJ>(g, b, sa, w, p0_next, vd_next);
 }

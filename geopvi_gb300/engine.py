@@ -49,7 +49,7 @@ class Fwi2dEngine:
 
     def __init__(self, params: Params, device=None, max_resident: int | None = None,
                  hbm_budget: int | None = None, graph: bool = True, plain: bool = False,
-                 checkpoint: bool = False):
+                 checkpoint: bool = False, variant: int | None = None):
         self.params = params
         self.lib = _native.load()
         self.device = torch.device(device if device is not None else "cuda")
@@ -63,6 +63,7 @@ class Fwi2dEngine:
         self.graph = graph
         self.plain = plain
         self.checkpoint = checkpoint
+        self.variant = variant  # FD step kernel variant; None: the library's tuner picks
         self._cp = params.c()
         self._work: torch.Tensor | None = None
         self._work_key = None
@@ -155,6 +156,8 @@ class Fwi2dEngine:
             flags |= _native.FLAG_FORWARD_ONLY
             want_grad = False
             want_syn = True
+        if self.variant is not None:
+            flags |= _native.flag_variant(self.variant)
         work, resident = self._workspace(n, flags)
         bufs = out if out is not None else self._outs.setdefault((n, want_grad, want_syn), {})
         if "misfit" not in bufs:
@@ -176,6 +179,17 @@ class Fwi2dEngine:
         _native.check(st, "gb_fwi2d_batch")
         return RunResult(misfit=misfit, grad=grad, syn=syn,
                          launches=int(self.lib.gb_fwi2d_last_launch_count()))
+
+    def tuned_variant(self, nsamples: int, *, imaging: bool = False, forward_only: bool = False,
+                      exact: bool = False) -> int:
+        """The FD step variant the tuner settled on for batches of ``nsamples``
+        run with the given mode (-1 while variants remain untried)."""
+        flags = (_native.FLAG_IMAGING if imaging else 0) | (_native.FLAG_PLAIN if self.plain else 0) | \
+            (_native.FLAG_CHECKPOINT if self.checkpoint else 0) | \
+            (_native.FLAG_FORWARD_ONLY if forward_only else 0) | (_native.FLAG_EXACT_GRADIENT if exact else 0)
+        _, resident = self._workspace(nsamples, flags)
+        with torch.cuda.device(self.device):
+            return int(self.lib.gb_fwi2d_tuned_variant(ctypes.byref(self._cp), nsamples, resident, flags))
 
     def status(self) -> int:
         """Device status word of the current workspace after the queued work

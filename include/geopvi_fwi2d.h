@@ -61,6 +61,13 @@ typedef struct gb_fwi2d_params {
                                     stored-field memory; results identical to full storage */
 #define GB_FWI2D_FORWARD_ONLY 0x10u /* synthetic data only (forward_2D): no adjoint, no stored field */
 #define GB_FWI2D_PROFILE 0x20u   /* time the step-kernel loops with CUDA events (not with GRAPH) */
+/* Kernel variant of the FD time step (bits 8-11): 0 lets the library's tuner
+ * choose -- the first calls with a given geometry, batch size, wave size and mode
+ * each time one variant on the caller's own batch, later calls run the fastest;
+ * GB_FWI2D_VARIANT(v) forces variant v (0-3).  Every variant computes the same
+ * values bit for bit. */
+#define GB_FWI2D_VARIANT_SHIFT 8
+#define GB_FWI2D_VARIANT(v) ((unsigned)((v) + 1) << GB_FWI2D_VARIANT_SHIFT)
 #define GB_FWI2D_EXACT_GRADIENT 0x40u /* grad = dJ/dv of J = 0.5*sum((syn-obs)^2), the exact discrete
                                         adjoint of the FD scheme (FP32), instead of backward_IO's
                                         gradient.  No counterpart in the reference.  Not with IMAGING;
@@ -153,6 +160,11 @@ long long gb_fwi2d_last_launch_count(void);
  * of those step kernels in milliseconds (negative if there were none) and in
  * *launches the number of step-kernel launches covered, then clears them. */
 double gb_fwi2d_profile_step_ms(long long *launches);
+
+/* The FD step variant the tuner settled on for this geometry, batch size
+ * (nsamples), wave size (max_resident as passed to gb_fwi2d_batch) and flags:
+ * 0-3, or -1 while variants remain untried.  No counterpart in the reference. */
+int gb_fwi2d_tuned_variant(const gb_fwi2d_params *p, int nsamples, int max_resident, unsigned flags);
 
 /* Release cached device tables and CUDA graphs held by the library. */
 void gb_fwi2d_release_caches(void);
