@@ -179,3 +179,18 @@ def test_checkpointing_is_bit_identical_to_full_storage(engine_lib, cuda, name):
         assert np.array_equal(o["syn"], ref["syn"]), kw
         assert np.array_equal(o["grad"], ref["grad"]), kw
         assert np.array_equal(o["misfit"], ref["misfit"]), kw
+
+
+@pytest.mark.parametrize("name", ["fwi_o8", "fwi_o12", "fwi_ragged"])
+def test_errors_against_fp64_oracle(engine_lib, cuda, oracle, name):
+    """The FP32 engine against the FP64 restatement of the same scheme: the
+    error of FP32 arithmetic itself (the reference is FP32 and matched bit for
+    bit above).  Reported bounds, as for the FP64 oracle against the reference."""
+    z = load(name)
+    p = cases.params_from_npz(z)
+    op = oracle.Params(**cases.params_to_dict(p))
+    syn64, grad64 = oracle.fwi_f64(op, z["start"].astype(np.float64), z["obs"].astype(np.float64), 1)
+    out = run(engine_for(p, graph=False), z["start"], z["obs"], want_syn=True)
+    e_syn, e_grad = rel(out["syn"][0], syn64), rel(out["grad"][0], grad64)
+    print(f"{name}: FP32 engine vs FP64 oracle: data {e_syn:.2e}, gradient {e_grad:.2e}")
+    assert e_syn < 1e-4 and e_grad < 1e-3
