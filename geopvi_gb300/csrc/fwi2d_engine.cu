@@ -238,6 +238,7 @@ struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
     size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
     size_t store, lam, gpad;  // exact gradient only: forward levels, adjoint levels, padded dJ/dv
+    size_t abeta, cells;      // exact gradient only: per-sample (v dt)^2 beta, the geometry's cell table
     size_t spec;              // pseudo-spectral mode: real field + half spectrum per resident solve
     int resident;
     int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
@@ -277,6 +278,8 @@ static Layout plan_layout_exact(const Geom &g, int nsamples, int resident, bool 
     L.store = off;  off = align256(off + field * (L.ckpt_k + 1) * resident);
     L.lam = off;    off = align256(off + field * 3 * resident);
     L.gpad = off;   off = align256(off + field * ninst);
+    L.abeta = off;  off = align256(off + field * nsamples);
+    L.cells = off;  off = align256(off + sizeof(int4) * (size_t)g.ntz * g.ntx);
     L.psave = L.gacc = off;
     L.syn = off;
     if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
@@ -833,7 +836,11 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     const size_t ring_pitch = 3 * fbytes, store_pitch = (size_t)(K + 1) * fbytes, ck_pitch = 2 * (size_t)nseg * fbytes;
 
     k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt, c.nsamples);
-    ++launches;
+    float *abeta = (float *)(c.work + L.abeta);
+    int4 *cells = (int4 *)(c.work + L.cells);
+    k_exact_tables<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.tab.coef, vdt, c.nsamples,
+                                                                                   cells, abeta);
+    launches += 2;
     cudaMemsetAsync(status, 0, sizeof(int), st);
     cudaMemsetAsync(gpad, 0, fbytes * ninst, st);
 
@@ -848,6 +855,8 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     b.status = status;
     ExactBatch x;
     x.vdt = vdt;
+    x.abeta = abeta;
+    x.cells = cells;
     x.obs = c.obs;
     x.syn = syn;
     x.lam = lam;

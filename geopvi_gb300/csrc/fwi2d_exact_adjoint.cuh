@@ -27,6 +27,8 @@ namespace gbfwi {
 
 struct ExactBatch {
     const float *vdt;      // [nsamples][fstride] padded v*dt
+    const float *abeta;    // [nsamples][fstride] (v dt)^2 beta on stencil cells, 0 elsewhere
+    const int4 *cells;     // [ntz][ntx] packed CellInfo of the geometry (cell_pack)
     const float *obs;      // [ns][nt][nr]
     const float *syn;      // [nsamples*ns][nt][nr]
     float *lam;            // [resident][3][fstride] adjoint levels
@@ -70,16 +72,50 @@ __device__ __forceinline__ CellInfo cell_info(const Geom &g, const BlendCoef *co
     return ci;
 }
 
-// beta_c of a stencil-region cell, 0 elsewhere (and off the grid).
-__device__ __forceinline__ float stencil_beta(const Geom &g, const BlendCoef *coef, int iz, int ix)
+// CellInfo packed into 16 bytes: x = sten | nb << 1 | (dir0 + 1) << 4 |
+// (dir1 + 1) << 8, then beta, gam0, gam1 as float bits.  The same for every
+// sample of a geometry, so it is built once and read through the cache.
+__device__ __forceinline__ int4 cell_pack(const CellInfo &c)
 {
-    if (iz < g.Lc || iz >= g.ntz - g.Lc || ix < g.Lc || ix >= g.ntx - g.Lc) return 0.0f;
-    float beta = 1.0f;
-    if (iz < g.pml) beta = 1.0f - coef[iz - g.Lc].w;
-    else if (iz >= g.ntz - g.pml) beta = 1.0f - coef[g.ntz - g.Lc - iz - 1].w;
-    if (ix < g.pml) beta *= 1.0f - coef[ix - g.Lc].w;
-    else if (ix >= g.ntx - g.pml) beta *= 1.0f - coef[g.ntx - g.Lc - ix - 1].w;
-    return beta;
+    return make_int4((c.sten ? 1 : 0) | (c.nb << 1) | ((c.dir[0] + 1) << 4) | ((c.dir[1] + 1) << 8),
+                     __float_as_int(c.beta), __float_as_int(c.gam[0]), __float_as_int(c.gam[1]));
+}
+
+__device__ __forceinline__ CellInfo cell_unpack(int4 v)
+{
+    CellInfo c;
+    c.sten = (v.x & 1) != 0;
+    c.nb = (v.x >> 1) & 3;
+    c.dir[0] = ((v.x >> 4) & 15) - 1;
+    c.dir[1] = ((v.x >> 8) & 15) - 1;
+    c.beta = __int_as_float(v.y);
+    c.gam[0] = __int_as_float(v.z);
+    c.gam[1] = __int_as_float(v.w);
+    return c;
+}
+
+// The geometry's cell table and each sample's (v dt)^2 beta field.
+__global__ void k_exact_tables(const Geom g, const BlendCoef *coef, const float *__restrict__ vdt, int nsamples,
+                               int4 *__restrict__ cells, float *__restrict__ abeta)
+{
+    const long long n = (long long)g.ntz * g.ntx;
+    for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
+         d += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(d / g.ntx), ix = (int)(d - (long long)iz * g.ntx);
+        cells[d] = cell_pack(cell_info(g, coef, iz, ix));
+    }
+    const long long m = (long long)nsamples * g.fstride;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e % g.fstride;
+        const int iz = (int)(r / g.pitch), ix = (int)(r - (long long)iz * g.pitch) - g.xoff;
+        float a = 0.0f;
+        if (ix >= 0 && ix < g.ntx) {
+            const CellInfo c = cell_info(g, coef, iz, ix);
+            if (c.sten) a = vdt[e] * vdt[e] * c.beta;
+        }
+        abeta[e] = a;
+    }
 }
 
 // Extrapolation weights of s = v dt / dx (abc_for_p's t11, t12, t13).
@@ -126,14 +162,13 @@ __global__ void __launch_bounds__(256)
             out += b.syn[(long long)inst * g.nt * g.nr + t] - b.obs[(long long)shot * g.nt * g.nr + t];
         }
     }
-    const CellInfo cj = cell_info(g, b.coef, iz, ix);
+    const CellInfo cj = cell_unpack(b.cells[(long long)iz * g.ntx + ix]);
     // A1^T lambda^{k+1}: nu_c = a_c beta_c lambda_c over the stencil cells c reading j
+    const float *ab = b.abeta + (long long)sample * g.fstride;
     auto nu = [&](int cz, int cx) -> float {
-        const float beta = stencil_beta(g, b.coef, cz, cx);
-        if (beta == 0.0f) return 0.0f;
+        if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) return 0.0f;
         const long long c = (long long)cz * P + cx + g.xoff;
-        const float vd = vdt[c];
-        return vd * vd * beta * lam1[c];
+        return ab[c] * lam1[c];
     };
     if (cj.sten) {
         out += 2.0f * cj.beta * lam1[j] + fd_weight<H>(0) * (rdx2 + rdz2) * nu(iz, ix);
@@ -155,7 +190,7 @@ __global__ void __launch_bounds__(256)
             for (int kk = 0; kk <= 4; ++kk) {
                 const int cz = iz - kk * sz, cx = ix - kk * sx;
                 if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) continue;
-                const CellInfo c = cell_info(g, b.coef, cz, cx);
+                const CellInfo c = cell_unpack(b.cells[(long long)cz * g.ntx + cx]);
                 const float gam = c.dir[0] == d ? c.gam[0] : c.dir[1] == d ? c.gam[1] : 0.0f;
                 if (gam == 0.0f) continue;
                 const long long ci = (long long)cz * P + cx + g.xoff;
