@@ -235,16 +235,14 @@ def load_traffic(p, nres_avg: float):
 
 def run_gpu(args):
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
+    from geopvi_gb300.replicas import ReplicaGroup
+
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    grp = ReplicaGroup(dev)  # replicas: one batch per rank, host-side barrier and max-time only
+    world, rank = grp.world, grp.rank
 
     from geopvi_gb300.engine import Fwi2dEngine
     w = workload(args.config, args.nt)
@@ -256,9 +254,7 @@ def run_gpu(args):
     obs = eng.run(torch.from_numpy(w.truth).to(dev).unsqueeze(0), zeros, forward_only=True).syn[0].clone()
     nsamples = vel.shape[0]
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
+    barrier = grp.barrier
 
     for _ in range(args.warmup):
         eng.run(vel, obs, profile=True)
@@ -285,13 +281,10 @@ def run_gpu(args):
     step_ms, step_launches = eng.step_profile()
     device_status = eng.status()
     step_variant = eng.tuned_variant(nsamples)  # -1: the tuner was still trying variants
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = grp.max_seconds(ms / 1e3) * 1e3
     cu_batch = cell_updates_per_sample(p) * nsamples
-    value = args.steps * cu_batch * world / (ms_max / 1e3)
-    sgrad = args.steps * nsamples * world / (ms_max / 1e3)
+    value = grp.throughput(args.steps * cu_batch, ms_max / 1e3)
+    sgrad = grp.throughput(args.steps * nsamples, ms_max / 1e3)
 
     # roofline of the time-step kernel
     alg_total = algorithmic_bytes_per_sample(p) * nsamples * args.steps
@@ -353,10 +346,7 @@ def run_gpu(args):
                 loss, grad = post.fwi(x)
             t1 = time.perf_counter()
             e2e_s = t1 - t0
-            tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-            if world > 1:
-                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_s = float(tt.item())
+            e2e_s = grp.max_seconds(e2e_s)
             e2e = {"value": args.steps * cu_batch * world / e2e_s, "unit": "cell-updates/s",
                    "h2d_bytes_per_step": int(x.numel() * 8), "d2h_bytes_per_step": int(loss.nbytes + grad.nbytes),
                    "api": "geopvi_gb300.posterior.Posterior.fwi (host float64 in, numpy out)",
@@ -388,8 +378,7 @@ def run_gpu(args):
             "gpu_launches": launches, "device_status": device_status,
         }
         print(json.dumps(out), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    grp.close()
 
 
 # ---------------------------------------------------------------------------
