@@ -194,3 +194,23 @@ def test_errors_against_fp64_oracle(engine_lib, cuda, oracle, name):
     e_syn, e_grad = rel(out["syn"][0], syn64), rel(out["grad"][0], grad64)
     print(f"{name}: FP32 engine vs FP64 oracle: data {e_syn:.2e}, gradient {e_grad:.2e}")
     assert e_syn < 1e-4 and e_grad < 1e-3
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("config", ["cfg2", "cfg3"])
+def test_full_geometry_two_shots(engine_lib, cuda, oracle, config):
+    """The bench's own grids at full size (200x400 / nt 3000 and 300x600 / nt 4000,
+    dt 0.8 ms) on a two-shot subset: forward data and synthetic data bit for bit
+    against the FP32 oracle, gradient within the bar."""
+    from geopvi_gb300 import workloads
+    w = getattr(workloads, config)()
+    p = w.params.replace(ns=2)
+    op = oracle.Params(**cases.params_to_dict(p))
+    obs_o = oracle.forward_f32(op, w.truth)
+    fwd = run(engine_for(p, graph=False), w.truth, np.zeros(p.data_len, np.float32), forward_only=True)
+    assert np.array_equal(fwd["syn"][0], obs_o)
+    syn_o, grad_o = oracle.fwi_f32(op, w.samples[0], obs_o, 1)
+    out = run(engine_for(p, graph=False), w.samples[0], obs_o, want_syn=True)
+    assert np.array_equal(out["syn"][0], syn_o)
+    e = rel(out["grad"][0], grad_o)
+    assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
