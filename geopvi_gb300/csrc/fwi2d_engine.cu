@@ -170,6 +170,32 @@ static void wavenumber(int ntx, int ntz, float dx, float dz, std::vector<float> 
         }
 }
 
+// Memory column of padded ix = 0.  The step kernel's 32-column tiles are
+// rim-only (no column in [Lc, ntx - Lc): zeros stored, no stencil), interior
+// (every column in [pml, ntx - pml): the lean sweep) or general (absorbing
+// strips: per-cell region tests and blends for the whole warp, about 2.5x
+// an interior tile).  The offset minimises that cost; the smallest wins ties.
+static int column_offset(int ntx, int Lc, int pml)
+{
+    int best = 0;
+    long long best_cost = -1;
+    for (int xoff = 0; xoff < kTileX; ++xoff) {
+        const int tiles = (xoff + ntx + kTileX - 1) / kTileX;
+        long long cost = 0;
+        for (int t = 0; t < tiles; ++t) {
+            const int lo = t * kTileX - xoff, hi = lo + kTileX;
+            if (hi <= Lc || lo >= ntx - Lc) cost += 1;
+            else if (lo >= pml && hi <= ntx - pml) cost += 4;
+            else cost += 10;
+        }
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = xoff;
+        }
+    }
+    return best;
+}
+
 static int derive(const gb_fwi2d_params &p, Derived &d)
 {
     int st = validate(p);
@@ -181,12 +207,14 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     g.pml0 = p.pml0;
     g.ntz = p.nz + 2 * g.pml;
     g.ntx = p.nx + 2 * g.pml;
-    // Column offset so that the interior (ix = pml) starts on a 128-byte line.
-    g.xoff = (kTileX - g.pml % kTileX) % kTileX;
+    g.xoff = column_offset(g.ntx, g.Lc, g.pml);
     g.pitch = round_up(g.xoff + g.ntx, kTileX);
     g.nx = p.nx;
     g.nz = p.nz;
-    g.ipitch = round_up(p.nx, kTileX);
+    // Interior arrays (snapshots, gradient sums) share the tiles' 128-byte
+    // lines: interior column 0 sits at the memory column of padded ix = pml.
+    g.ioff = (g.xoff + g.pml) % kTileX;
+    g.ipitch = round_up(g.ioff + p.nx, kTileX);
     g.s_iz = g.pml + p.depths;
     g.r_iz = g.pml + p.depthr;
     g.r_ix0 = g.pml + p.nr0;
@@ -362,7 +390,7 @@ __global__ void k_reduce_grad(const Geom g, const float *__restrict__ gacc,
         const int s = (int)(e / cells);
         const long long k = e - (long long)s * cells;
         const int iz = (int)(k / g.nx), ix = (int)(k - (long long)iz * g.nx);
-        const long long pc = (long long)iz * g.ipitch + ix;
+        const long long pc = (long long)iz * g.ipitch + ix + g.ioff;
         double acc = 0.0;
         for (int shot = 0; shot < g.ns; ++shot)
             acc += (double)gacc[((long long)s * g.ns + shot) * g.pstride + pc];
@@ -519,7 +547,7 @@ template <int H, int U, int MINB>
 static void launch_step_variant(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
                                 const StepArgs &sa, cudaStream_t st)
 {
-    const dim3 grid(g.tiles_x * g.tiles_z, nres), block(kThreads);
+    const dim3 grid(nres, g.tiles_x * g.tiles_z), block(kThreads);
     const int smem = TileShape<H>::kSmem;
     if (adj)
         k_step<H, true, U, MINB><<<grid, block, smem, st>>>(m.p1, g, b, sa);

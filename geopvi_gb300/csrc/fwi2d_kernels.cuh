@@ -90,6 +90,7 @@ struct Geom {
     int ntx, ntz;        // padded grid (fdtd2D_modelling.c:86-87)
     int pitch, xoff;     // row pitch in floats; memory column of padded ix = 0
     int nx, nz, ipitch;  // interior grid and the row pitch of interior arrays
+    int ioff;            // memory column of interior ix = pml in interior arrays
     int pml, Lc, pml0;   // Lc here is the reference's Lc after Lc += 1
     int s_iz, r_iz, r_ix0, dr, nr;
     int ds, s_ix0;       // source column of shot is: s_ix0 + is*ds
@@ -498,8 +499,8 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
     }
 }
 
-// One time step of every solve in the wave.  blockIdx.x = tile, blockIdx.y =
-// resident slot.  tm_p1 views the ring as [3*resident][ntz][pitch] with a
+// One time step of every solve in the wave, one block per (resident slot,
+// tile).  tm_p1 views the ring as [3*resident][ntz][pitch] with a
 // (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
 // and v*dt are read once per cell with coalesced read-only loads (the
 // boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
@@ -516,12 +517,33 @@ __global__ void __launch_bounds__(kThreads, MINB)
     float *s1 = smem;
     uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
 
-    const int slot = blockIdx.y;
-    const int tcol = blockIdx.x % g.tiles_x;
-    const int trow = blockIdx.x / g.tiles_x;
+    // blockIdx.x = solve, blockIdx.y = tile rank.  Ranks visit tile rows and
+    // columns from the edges inward, so the tiles with absorbing strips (the
+    // longest) of every solve are dispatched first and each launch ends on
+    // interior tiles: a short tail before the next step.
+    const int slot = blockIdx.x;
+    const int rr = blockIdx.y / g.tiles_x, cr = blockIdx.y - rr * g.tiles_x;
+    const int trow = (rr & 1) ? g.tiles_z - 1 - (rr >> 1) : (rr >> 1);
+    const int tcol = (cr & 1) ? g.tiles_x - 1 - (cr >> 1) : (cr >> 1);
     const int col0 = tcol * kTileX;
     const int row0 = trow * kTileZ;
     const int b0 = sa.k % 3, b1 = (sa.k + 1) % 3, b2 = (sa.k + 2) % 3;
+
+    // Tiles with no column in [Lc, ntx - Lc): the rim, which neither the
+    // stencil nor abc_for_p's passes change from its initial zero (the top and
+    // bottom passes blend rim columns from rim neighbours only), so the new
+    // level is zero there.  Block-uniform; no staging.
+    if (col0 - g.xoff + kTileX <= g.Lc || col0 - g.xoff >= g.ntx - g.Lc) {
+        const int ix = col0 - g.xoff + (threadIdx.x & 31);
+        if (ix >= 0 && ix < g.ntx) {
+            float *p2 = b.ring + ((long long)slot * 3 + b2) * g.fstride + col0 + (threadIdx.x & 31);
+            const int iz0 = row0 + (threadIdx.x >> 5) * kWarpRows;
+#pragma unroll 4
+            for (int j = 0; j < kWarpRows; ++j)
+                if (iz0 + j < g.ntz) p2[(long long)(iz0 + j) * g.pitch] = 0.0f;
+        }
+        return;
+    }
 
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -572,8 +594,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
     w.ps = nullptr;
     w.G = nullptr;
     if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
-        w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml);
-        if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml);
+        w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml + g.ioff);
+        if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml + g.ioff);
     }
     // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
     const int ix0 = col0 - g.xoff;

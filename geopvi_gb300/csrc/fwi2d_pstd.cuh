@@ -129,11 +129,11 @@ __global__ void __launch_bounds__(256) k_step_pstd(const Geom g, const Batch b, 
     if (sa.snap >= 0 && (ADJ || b.store) && iz >= g.pml && iz < g.ntz - g.pml && ix >= g.pml &&
         ix < g.ntx - g.pml) {
         const long long pc = ((long long)slot * g.nt_save + sa.snap) * g.pstride + (long long)(iz - g.pml) * g.ipitch +
-                             (ix - g.pml);
+                             (ix - g.pml + g.ioff);
         if (!ADJ) {
             b.psave[pc] = b.imaging ? q : div2_any(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
         } else {
-            float *G = b.gacc + (long long)inst * g.pstride + (long long)(iz - g.pml) * g.ipitch + (ix - g.pml);
+            float *G = b.gacc + (long long)inst * g.pstride + (long long)(iz - g.pml) * g.ipitch + (ix - g.pml + g.ioff);
             *G = fa(*G, fm(b.psave[pc], q));
         }
     }
