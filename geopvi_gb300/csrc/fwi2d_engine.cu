@@ -538,33 +538,48 @@ struct Maps {
     CUtensorMap p1;
 };
 
+// First failure status of the launches being enqueued on this thread.
+static thread_local int t_enqueue_error = 0;
+
 static bool make_maps(Maps &m, const Geom &g, float *ring, int resident)
 {
     return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * (g.Lc - 1));
 }
 
+// overlap: the previous operation on `st` is the step before this one, and
+// this step may be launched programmatically (its blocks become resident
+// while that step drains; k_step waits on it before any global access).
 template <int H, int U, int MINB>
 static void launch_step_variant(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
-                                const StepArgs &sa, cudaStream_t st)
+                                const StepArgs &sa, cudaStream_t st, bool overlap)
 {
-    const dim3 grid(nres, g.tiles_x * g.tiles_z), block(kThreads);
-    const int smem = TileShape<H>::kSmem;
-    if (adj)
-        k_step<H, true, U, MINB><<<grid, block, smem, st>>>(m.p1, g, b, sa);
-    else
-        k_step<H, false, U, MINB><<<grid, block, smem, st>>>(m.p1, g, b, sa);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nres, g.tiles_x * g.tiles_z);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = TileShape<H>::kSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlap ? 1 : 0;
+    const cudaError_t e = adj ? cudaLaunchKernelEx(&cfg, k_step<H, true, U, MINB>, m.p1, g, b, sa)
+                              : cudaLaunchKernelEx(&cfg, k_step<H, false, U, MINB>, m.p1, g, b, sa);
+    if (e != cudaSuccess) t_enqueue_error = GB_FWI2D_ECUDA;
 }
 
 template <int H>
 static void launch_step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres,
-                        const StepArgs &sa, cudaStream_t st, int variant)
+                        const StepArgs &sa, cudaStream_t st, int variant, bool overlap)
 {
     static_assert(kNumStepVariants == 4, "one case per entry of kStepVariants");
+    constexpr StepVariant v1 = kStepVariants[1], v2 = kStepVariants[2], v3 = kStepVariants[3],
+                          v0 = kStepVariants[0];
     switch (variant) {
-    case 1: launch_step_variant<H, kStepVariants[1].rows, kStepVariants[1].min_blocks>(adj, m, g, b, nres, sa, st); break;
-    case 2: launch_step_variant<H, kStepVariants[2].rows, kStepVariants[2].min_blocks>(adj, m, g, b, nres, sa, st); break;
-    case 3: launch_step_variant<H, kStepVariants[3].rows, kStepVariants[3].min_blocks>(adj, m, g, b, nres, sa, st); break;
-    default: launch_step_variant<H, kStepVariants[0].rows, kStepVariants[0].min_blocks>(adj, m, g, b, nres, sa, st); break;
+    case 1: launch_step_variant<H, v1.rows, v1.min_blocks>(adj, m, g, b, nres, sa, st, overlap); break;
+    case 2: launch_step_variant<H, v2.rows, v2.min_blocks>(adj, m, g, b, nres, sa, st, overlap); break;
+    case 3: launch_step_variant<H, v3.rows, v3.min_blocks>(adj, m, g, b, nres, sa, st, overlap); break;
+    default: launch_step_variant<H, v0.rows, v0.min_blocks>(adj, m, g, b, nres, sa, st, overlap); break;
     }
 }
 
@@ -604,7 +619,6 @@ static const CufftApi *cufft_api()
 
 static std::map<std::tuple<int, int, int, int, int>, cufftHandle> g_fft_plans;  // (device, ntz, ntx, batch, dir)
 static std::map<std::tuple<int, int, int, uint32_t, uint32_t>, float *> g_kk_tables;  // (device, ntz, ntx, dx, dz)
-static thread_local int t_enqueue_error = 0;
 
 // Batched 2-D plans for `batch` fields: real [ntz][ntx] -> half spectrum
 // [ntz][ntx/2+1] (forward, D2Z) or back (inverse, Z2D), out of place.
@@ -692,14 +706,14 @@ static int step_pstd(bool adj, const Geom &g, const Batch &b, int nres, const St
 
 // One time step of the wave; returns the number of this library's kernels.
 static int step(bool adj, const Maps &m, const Geom &g, const Batch &b, int nres, const StepArgs &sa,
-                cudaStream_t st, int variant)
+                cudaStream_t st, int variant, bool overlap = false)
 {
     if (g.pstd) return step_pstd(adj, g, b, nres, sa, st);
     switch (g.Lc - 1) {
-    case 3: launch_step<3>(adj, m, g, b, nres, sa, st, variant); break;
-    case 4: launch_step<4>(adj, m, g, b, nres, sa, st, variant); break;
-    case 5: launch_step<5>(adj, m, g, b, nres, sa, st, variant); break;
-    default: launch_step<6>(adj, m, g, b, nres, sa, st, variant); break;
+    case 3: launch_step<3>(adj, m, g, b, nres, sa, st, variant, overlap); break;
+    case 4: launch_step<4>(adj, m, g, b, nres, sa, st, variant, overlap); break;
+    case 5: launch_step<5>(adj, m, g, b, nres, sa, st, variant, overlap); break;
+    default: launch_step<6>(adj, m, g, b, nres, sa, st, variant, overlap); break;
     }
     return 1;
 }
@@ -1033,7 +1047,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
                 sa.it = adj ? g.nt - 1 - k : k;
                 sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
                 sa.rik = adj ? 0.0f : c.d->rik[sa.it];
-                launches += step(adj, maps, g, b, nres, sa, st, variant);
+                launches += step(adj, maps, g, b, nres, sa, st, variant, k > 0);
             }
             if (e1) {
                 cudaEventRecord(e1, st);

@@ -230,6 +230,12 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
 
 // Bounded wait: true once phase `parity` completed, false after the limit
 // (the caller records the timeout and skips its work).
+// Programmatic dependent launch: wait for the previous grid on the stream
+// (complete, its writes visible), and let the next one be scheduled.  Both
+// are no-ops in a launch without the programmatic-serialization attribute.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
 {
     for (int i = 0; i < (1 << 24); ++i)
@@ -534,6 +540,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
     // bottom passes blend rim columns from rim neighbours only), so the new
     // level is zero there.  Block-uniform; no staging.
     if (col0 - g.xoff + kTileX <= g.Lc || col0 - g.xoff >= g.ntx - g.Lc) {
+        grid_dependency_wait();
+        grid_launch_dependents();
         const int ix = col0 - g.xoff + (threadIdx.x & 31);
         if (ix >= 0 && ix < g.ntx) {
             float *p2 = b.ring + ((long long)slot * 3 + b2) * g.fstride + col0 + (threadIdx.x & 31);
@@ -550,6 +558,11 @@ __global__ void __launch_bounds__(kThreads, MINB)
         fence_barrier_init();
     }
     __syncthreads();
+    // Everything above touched no global memory; the previous step (which
+    // writes p1 and reads the buffer p2 overwrites) must be complete below.
+    // Its successor may be scheduled once every block of this one is past here.
+    grid_dependency_wait();
+    grid_launch_dependents();
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&bar, TS::kBytes);
         tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
