@@ -295,14 +295,21 @@ def run_gpu(args):
         peaks = json.load(open(pk_path))
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # step_launches counts time steps of a wave; a wave of many resident
+    # solves runs each step as two concurrent launches (one per half of the
+    # solves, on two streams), so the per-step figures cover both.
     avg_launch_ms = step_ms / max(step_launches, 1)
     ninst = nsamples * p.ns
+    waves = -(-ninst // resident)
+    # kernels per run: k_prepare, the step launches, the gradient reduction, two misfit kernels
+    kernels_per_step = (launches / args.steps - 4) / (waves * 2 * p.nt)
     nres_avg = ninst * 2 * p.nt * args.steps / max(step_launches, 1)
     traffic = load_traffic(p, nres_avg)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_src, "kernel": "k_step (fused FD step)",
                 "avg_launch_ms": avg_launch_ms, "step_share_of_region": step_ms / ms if ms else None,
-                "algorithmic_bytes_per_launch": alg_total / max(step_launches, 1)}
+                "algorithmic_bytes_per_launch": alg_total / max(step_launches, 1),
+                "per": "time step of a wave", "kernel_launches_per_time_step": round(kernels_per_step, 3)}
 
     # plain comparator: one (sample, shot) per launch, shots in order, one sample
     plain = None

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -541,6 +542,43 @@ struct Maps {
 // First failure status of the launches being enqueued on this thread.
 static thread_local int t_enqueue_error = 0;
 
+// Second stream of the main loop's two-halves schedule, per (device, host
+// thread), with its fork / join events.  Kept for the process (a graph
+// capture records work on it) and freed by gb_fwi2d_release_caches.
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static std::mutex g_side_mutex;
+static std::map<std::pair<int, std::thread::id>, SideStream> g_side;
+
+// This thread's side stream on the current device; created on first use
+// unless `create` is false (a stream being captured by the caller).
+static const SideStream *side_stream(bool create)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_side_mutex);
+    const auto key = std::make_pair(dev, std::this_thread::get_id());
+    auto it = g_side.find(key);
+    if (it != g_side.end()) return &it->second;
+    if (!create) return nullptr;
+    SideStream ss;
+    if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess) {
+        if (ss.fork) cudaEventDestroy(ss.fork);
+        cudaStreamDestroy(ss.s);
+        return nullptr;
+    }
+    return &(g_side[key] = ss);
+}
+
+// Waves of at least this many resident solves run as two halves on two
+// streams: each half's steps form their own chain, so the ramp and tail of
+// one half's launches overlap the other half's work.
+constexpr int kSplitMinResident = 32;
+
 static bool make_maps(Maps &m, const Geom &g, float *ring, int resident)
 {
     return make_map(m.p1, ring, g, 3LL * resident, kBoxX, kTileZ + 2 * (g.Lc - 1));
@@ -1013,9 +1051,14 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.spec = (double *)(c.work + c.L.spec);
     b.spec_resident = c.L.resident;
     b.kk = c.kk;
+    b.slot0 = 0;
     const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    const SideStream *side = (g.pstd || wave < kSplitMinResident) ? nullptr
+                                                                   : side_stream(cs == cudaStreamCaptureStatusNone);
     const bool ckpt = (c.flags & GB_FWI2D_CHECKPOINT) && !fwd_only;
     for (long long i0 = 0; i0 < ninst && ckpt; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
@@ -1041,13 +1084,26 @@ static long long enqueue(const Call &c, cudaStream_t st)
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (c.profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
                 cudaEventRecord(e0, st);
+            const bool split = side && nres >= kSplitMinResident;
+            const int nlo = split ? nres / 2 : nres;
+            Batch bhi = b;
+            bhi.slot0 = nlo;
+            if (split) {  // fork: the second half's chain on the side stream
+                cudaEventRecord(side->fork, st);
+                cudaStreamWaitEvent(side->s, side->fork, 0);
+            }
             for (int k = 0; k < g.nt; ++k) {
                 StepArgs sa;
                 sa.k = k;
                 sa.it = adj ? g.nt - 1 - k : k;
                 sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
                 sa.rik = adj ? 0.0f : c.d->rik[sa.it];
-                launches += step(adj, maps, g, b, nres, sa, st, variant, k > 0);
+                launches += step(adj, maps, g, b, nlo, sa, st, variant, k > 0);
+                if (split) launches += step(adj, maps, g, bhi, nres - nlo, sa, side->s, variant, k > 0);
+            }
+            if (split) {  // join
+                cudaEventRecord(side->join, side->s);
+                cudaStreamWaitEvent(st, side->join, 0);
             }
             if (e1) {
                 cudaEventRecord(e1, st);
@@ -1184,6 +1240,7 @@ static int run_graph(const Call &c, cudaStream_t st, long long &launches)
                                                                       : GB_FWI2D_ECUDA;
         }
     }
+    side_stream(true);  // created outside the capture
     cudaStream_t cap;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return GB_FWI2D_ECUDA;
     cudaGraph_t graph = nullptr;
@@ -1404,6 +1461,13 @@ void gb_fwi2d_release_caches(void)
     g_fft_plans.clear();
     for (auto &kv : g_kk_tables) cudaFree(kv.second);
     g_kk_tables.clear();
+    std::lock_guard<std::mutex> lk2(g_side_mutex);
+    for (auto &kv : g_side) {
+        cudaEventDestroy(kv.second.fork);
+        cudaEventDestroy(kv.second.join);
+        cudaStreamDestroy(kv.second.s);
+    }
+    g_side.clear();
 }
 
 }  // extern "C"

@@ -118,6 +118,7 @@ struct Batch {
     int blend_fp32;      // the host proved (1 - w) * q exact in double for every weight
     int *status;         // device error word (0 = ok)
     int inst0;           // first solve of this wave
+    int slot0;           // first resident slot of this launch (the wave's second half)
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
     double *spec;        // pseudo-spectral mode: [resident][ntz][ntx] real array, then the
@@ -527,7 +528,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
     // columns from the edges inward, so the tiles with absorbing strips (the
     // longest) of every solve are dispatched first and each launch ends on
     // interior tiles: a short tail before the next step.
-    const int slot = blockIdx.x;
+    const int slot = b.slot0 + blockIdx.x;
     const int rr = blockIdx.y / g.tiles_x, cr = blockIdx.y - rr * g.tiles_x;
     const int trow = (rr & 1) ? g.tiles_z - 1 - (rr >> 1) : (rr >> 1);
     const int tcol = (cr & 1) ? g.tiles_x - 1 - (cr >> 1) : (cr >> 1);
