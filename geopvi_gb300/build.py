@@ -47,7 +47,7 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB_PATH)
     deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    deps.append(os.path.join(REPO_DIR, "include", "geopvi_fwi2d.h"))
+    deps += [os.path.join(REPO_DIR, "include", h) for h in ("geopvi_fwi2d.h", "geopvi_fwi3d.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
