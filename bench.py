@@ -47,8 +47,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"],
-                    help="cfg4: uneven batch of 48 instances; cfg5: serving loop (own JSON line)")
+    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5", "fwi3d"],
+                    help="cfg4: uneven batch of 48 instances; cfg5: serving loop; fwi3d: the 3-D engine "
+                         "(each its own JSON line)")
     ap.add_argument("--requests", type=int, default=12, help="cfg5: requests served")
     ap.add_argument("--rate", type=float, default=200.0, help="cfg5: mean Poisson arrival rate (req/s)")
     ap.add_argument("--cpu-shots", type=int, default=2, help="shots in the bounded CPU sample")
@@ -514,6 +515,106 @@ def run_serving(args):
     }), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# fwi3d: the 3-D engine behind the fwi3d posterior boundary
+# ---------------------------------------------------------------------------
+def run_fwi3d(args):
+    """Misfit + gradient of a batch of 3-D models (workloads.fwi3d_workload):
+    device-timed engine runs, the same through the reference-compatible
+    Posterior with host arrays, the CPU oracle on one shot."""
+    import configparser
+    from types import SimpleNamespace
+    import torch
+    from geopvi_gb300 import fwi3d, workloads
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    w = workloads.fwi3d_workload(nt=args.nt or 600)
+    p = w.params
+    eng = fwi3d.Fwi3dEngine(p, w.src, w.rec, w.wavelet, device=dev)
+    obs = eng.run(torch.from_numpy(w.truth).to(dev).unsqueeze(0), forward_only=True).syn[0].contiguous()
+    vel = torch.from_numpy(w.samples).to(dev)
+    nsamples = vel.shape[0]
+    for _ in range(args.warmup):
+        r = eng.run(vel, obs)
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    e0.record()
+    for _ in range(args.steps):
+        r = eng.run(vel, obs)
+        launches += r.launches
+    e1.record()
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    resident = eng._resident
+    pad = 2 * (p.pml0 + p.Lc + 1)
+    ntp = (p.nx + pad) * (p.ny + pad) * (p.nz + pad)
+    ncell = p.nx * p.ny * p.nz
+    nt_save = -(-p.nt // p.nt_interval)
+    cu = 2 * p.ns * p.nt * ntp * nsamples * args.steps
+    alg = p.ns * nsamples * args.steps * (2 * p.nt * 16 * ntp + nt_save * 16 * ncell)
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg / (ms / 1e3) / 1e9
+    # end to end through the Posterior: host float64 models in, numpy loss and gradient out
+    e2e = None
+    with tempfile.TemporaryDirectory() as d:
+        for name, arr in (("source", w.src), ("data", obs.cpu().numpy()), ("rec", w.rec), ("wavelet", w.wavelet)):
+            np.save(os.path.join(d, name + ".npy"), arr)
+        cfg = configparser.ConfigParser()
+        cfg["FWI"] = dict(nx=str(p.nx), ny=str(p.ny), nz=str(p.nz), dx=str(p.dx), dy=str(p.dy), dz=str(p.dz),
+                          dt=str(p.dt), pml=str(p.pml0), Lc=str(p.Lc), shot_batch=str(p.ns), vel_fixed="1500",
+                          recfile=os.path.join(d, "rec.npy"), waveletfile=os.path.join(d, "wavelet.npy"))
+        cfg["path"] = dict(inpath=d, outpath=d, srcfile=os.path.join(d, "source.npy"),
+                           datafile=os.path.join(d, "data.npy"))
+        post = fwi3d.Posterior(SimpleNamespace(sigma=1.0), cfg, device=dev)
+        x = w.samples.astype(np.float64)
+        post.fwi3d(x)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            loss, grad = post.fwi3d(x)
+        wall = time.perf_counter() - t0
+        e2e = {"value": cu / wall, "unit": "cell-updates/s", "h2d_bytes_per_step": int(x.nbytes),
+               "d2h_bytes_per_step": int(loss.nbytes + grad.nbytes),
+               "api": "geopvi_gb300.fwi3d.Posterior.fwi3d (host float64 in, numpy out)"}
+        del post
+    del eng
+    torch.cuda.empty_cache()
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle3d as O3
+        sub_nt = min(p.nt, 150)
+        sp = p.replace(ns=1, nt=sub_nt)
+        obs_sub = O3.run(sp, w.src[:1], w.rec, w.wavelet[:sub_nt], w.truth)[0]
+        t0 = time.perf_counter()
+        O3.run(sp, w.src[:1], w.rec, w.wavelet[:sub_nt], w.samples[0], obs_sub, grad=True)
+        sec = time.perf_counter() - t0
+        cpu = {"value": 2 * sub_nt * ntp / sec, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 sample x 1 of {p.ns} shots, nt {sub_nt} of {p.nt} (cost is linear in shots and "
+                         f"steps); FP32 C++ oracle of the 3-D scheme, OpenMP", "seconds": sec}
+    print(json.dumps({
+        "metric": "FD cell-updates/s (3-D misfit+gradient, fwd+adjoint)", "value": cu / (ms / 1e3),
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded models)",
+        "config": {"workload": f"3-D batch: {p.nx}x{p.ny}x{p.nz} cells, nt {p.nt}, {p.ns} shots, {p.nr} receivers, "
+                               f"{nsamples} samples, 8th order", "resident_solves": resident,
+                   "waves": -(-(nsamples * p.ns) // resident),
+                   "l2": "inputs larger than L2 (one padded field is 28 MB; the stored field per solve ~10 GB)"},
+        "sample_gradients_per_s": nsamples * args.steps / (ms / 1e3),
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k3_step (3-D step) and its IO kernels, whole run",
+                     "algorithmic_bytes_per_step": alg / args.steps},
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+    }), flush=True)
+
+
 def main():
     args = parse_args()
     if args.warmup < 3:
@@ -524,6 +625,8 @@ def main():
         run_uneven(args)
     elif args.config == "cfg5":
         run_serving(args)
+    elif args.config == "fwi3d":
+        run_fwi3d(args)
     else:
         run_gpu(args)
 

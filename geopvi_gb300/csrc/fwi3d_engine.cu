@@ -33,9 +33,18 @@ namespace gbfwi3 {
 
 using gbfwi::fd_weight;
 
+// Build-time tuning knobs: planes per z chunk (each chunk reloads 2H planes
+// of the z window) and resident blocks per SM the registers are capped for.
+#ifndef GB_FWI3D_ZCHUNK
+#define GB_FWI3D_ZCHUNK 32
+#endif
+#ifndef GB_FWI3D_MIN_BLOCKS
+#define GB_FWI3D_MIN_BLOCKS 4
+#endif
+
 constexpr int kBX = 32;     // tile columns (x), one warp
 constexpr int kBY = 8;      // tile rows (y)
-constexpr int kZC = 32;     // planes per z chunk
+constexpr int kZC = GB_FWI3D_ZCHUNK;  // planes per z chunk
 constexpr int kMisfitBlocks = 64;
 
 struct Geom3 {
@@ -104,7 +113,7 @@ __device__ __forceinline__ float blend(float q, float s, float w, float omw, flo
 // (ring buffers (k, k+1, k+2) mod 3 = p0, p1, p2); snap >= 0: the slot's
 // stored-field index written (forward) or read (adjoint) at this step.
 template <int H, bool ADJ>
-__global__ void __launch_bounds__(kBX *kBY) k3_step(const Geom3 g, const Batch3 b, int k, int snap)
+__global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const Geom3 g, const Batch3 b, int k, int snap)
 {
     const int slot = blockIdx.y;
     int t = blockIdx.x;

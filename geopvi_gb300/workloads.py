@@ -152,3 +152,52 @@ def scaled(p: Params, *, nz: int | None = None, nx: int | None = None, nt: int |
     ns = ns or p.ns
     return make_params(nz, nx, nt or p.nt, p.dt, ns, p.f0, nr=min(p.nr, nx), dx=p.dx, Lc=p.Lc,
                        pml0=p.pml0, depths=p.depths, depthr=p.depthr, nt_interval=p.nt_interval)
+
+
+@dataclass
+class Workload3D:
+    """A seeded 3-D inversion batch for the 3-D engine (fwi3d)."""
+    name: str
+    params: object          # fwi3d.Fwi3dParams
+    src: np.ndarray         # (ns, 3) model cells
+    rec: np.ndarray         # (nr, 3) model cells
+    wavelet: np.ndarray     # (nt,)
+    truth: np.ndarray       # (ny*nx*nz,) float32, (ny, nx, nz) order
+    samples: np.ndarray     # (nsamples, ny*nx*nz) float32
+
+
+def ricker(nt: int, dt: float, f0: float) -> np.ndarray:
+    """Ricker wavelet (1 - 2a) exp(-a), a = (pi f0 (t - 1/f0))^2, in FP64 rounded to float32."""
+    t = np.arange(nt) * dt - 1.0 / f0
+    a = (np.pi * f0 * t) ** 2
+    return ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+
+
+def fwi3d_workload(n: int = 160, nt: int = 600, nsamples: int = 4, seed: int = 6) -> Workload3D:
+    """n^3 cells of 10 m, dt 1 ms, 8th order, 10-cell absorbing strips; 8 shots
+    on a 2 x 4 surface grid at 2 cells depth, receivers every 4 cells on the
+    surface; truth: 1.6-3.0 km/s layers bending with depth plus a slow sphere;
+    samples: the smoothed truth plus N(0, 100^2), clipped to [1500, 3000]."""
+    from .fwi3d import Fwi3dParams
+    rng = np.random.default_rng(seed)
+    p = Fwi3dParams(nx=n, ny=n, nz=n, nt=nt, dt=1e-3, dx=10.0, dy=10.0, dz=10.0, pml0=10, Lc=4, nt_interval=1)
+    sx = np.linspace(n // 8, n - 1 - n // 8, 4).astype(int)
+    sy = np.linspace(n // 4, n - 1 - n // 4, 2).astype(int)
+    src = np.array([[x, y, 2] for y in sy for x in sx])
+    g = np.arange(0, n, 4)
+    rec = np.array([[x, y, 0] for y in g for x in g])
+    z = np.arange(n)[None, None, :]
+    x = np.arange(n)[None, :, None]
+    y = np.arange(n)[:, None, None]
+    depth = z + 0.08 * n * np.sin(2 * np.pi * x / n) * np.cos(np.pi * y / n)
+    truth = 1600.0 + 1400.0 * np.clip(depth / n, 0, 1)
+    r2 = (x - n / 2) ** 2 + (y - n / 2) ** 2 + (z - 0.55 * n) ** 2
+    truth = truth - 300.0 * np.exp(-r2 / (0.12 * n) ** 2)
+    base = truth.copy()
+    for axis in range(3):  # separable box smoothing, 9 cells
+        c = np.cumsum(np.pad(base, [(5, 4) if a == axis else (0, 0) for a in range(3)], mode="edge"), axis=axis)
+        base = (np.take(c, range(9, c.shape[axis]), axis=axis) - np.take(c, range(0, c.shape[axis] - 9), axis=axis)) / 9
+    samples = np.clip(base[None] + 100.0 * rng.standard_normal((nsamples,) + base.shape), 1500.0, 3000.0)
+    wav = ricker(nt, p.dt, 10.0)
+    return Workload3D("fwi3d", p.replace(ns=src.shape[0], nr=rec.shape[0]), src, rec, wav,
+                      truth.astype(np.float32).ravel(), samples.reshape(nsamples, -1).astype(np.float32))
