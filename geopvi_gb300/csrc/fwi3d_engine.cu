@@ -41,6 +41,11 @@ using gbfwi::fd_weight;
 #ifndef GB_FWI3D_MIN_BLOCKS
 #define GB_FWI3D_MIN_BLOCKS 4
 #endif
+#ifndef GB_FWI3D_ZUNROLL
+#define GB_FWI3D_ZUNROLL 1
+#endif
+#define GB_FWI3D_PRAGMA(x) _Pragma(#x)
+#define GB_FWI3D_UNROLL(n) GB_FWI3D_PRAGMA(unroll n)
 
 constexpr int kBX = 32;     // tile columns (x), one warp
 constexpr int kBY = 8;      // tile rows (y)
@@ -127,9 +132,9 @@ __global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const G
     const int inst = b.inst0 + slot;
     const int sample = inst / g.ns;
     float *ring = b.ring + (long long)slot * 3 * g.fstride;
-    const float *p0 = ring + (long long)(k % 3) * g.fstride;
-    const float *p1 = ring + (long long)((k + 1) % 3) * g.fstride;
-    float *p2 = ring + (long long)((k + 2) % 3) * g.fstride;
+    const float *__restrict__ p0 = ring + (long long)(k % 3) * g.fstride;
+    const float *__restrict__ p1 = ring + (long long)((k + 1) % 3) * g.fstride;
+    float *__restrict__ p2 = ring + (long long)((k + 2) % 3) * g.fstride;
     const long long col = (long long)y * g.pitch + x;
     const int L = g.L;
     if (x < L || x >= g.ntx - L || y < L || y >= g.nty - L) {  // rim column: always zero
@@ -155,9 +160,19 @@ __global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const G
         const int zz = z0 - H + m;
         win[m] = (zz >= 0 && zz < g.ntz) ? __ldg(p1 + zz * g.sz + col) : 0.0f;
     }
+    // this plane's window value, p0 and v*dt, loaded one plane ahead
+    float wn = z0 + H < g.ntz ? __ldg(p1 + (z0 + H) * g.sz + col) : 0.0f;
+    float p0n = __ldg(p0 + z0 * g.sz + col), vdn = __ldg(vdc + z0 * g.sz);
+    GB_FWI3D_UNROLL(GB_FWI3D_ZUNROLL)
     for (int z = z0; z < z1; ++z) {
-        const int zn = z + H;
-        win[2 * H] = zn < g.ntz ? __ldg(p1 + zn * g.sz + col) : 0.0f;
+        win[2 * H] = wn;
+        const float p0c = p0n, vd = vdn;
+        if (z + 1 < z1) {
+            const int zn = z + 1 + H;
+            wn = zn < g.ntz ? __ldg(p1 + zn * g.sz + col) : 0.0f;
+            p0n = __ldg(p0 + (z + 1) * g.sz + col);
+            vdn = __ldg(vdc + (z + 1) * g.sz);
+        }
         const long long c = z * g.sz + col;
         float q = 0.0f;
         if (z >= L && z < g.ntz - L) {
@@ -172,9 +187,7 @@ __global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const G
             float tt = __fmul_rn(lz, g.id2[2]);
             tt = fmaf_rn(ly, g.id2[1], tt);
             tt = fmaf_rn(lx, g.id2[0], tt);
-            const float p0c = __ldg(p0 + c);
             const float u = fmaf_rn(2.0f, pc, -p0c);
-            const float vd = __ldg(vdc + z * g.sz);
             q = fmaf_rn(__fmul_rn(vd, vd), tt, u);
             const bool zmin = z < g.pml, zmax = z >= g.ntz - g.pml;
             if (zmin) {
