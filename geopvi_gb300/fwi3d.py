@@ -153,6 +153,14 @@ class Fwi3dEngine:
         self._work = None
         self._key = None
 
+    def set_sources(self, src) -> None:
+        """Replace the shot positions (same number of shots): the workspace is reused."""
+        acq = Acquisition(src, self.acq.rec, self.acq.wavelet)
+        if acq.src.shape[0] != self.params.ns:
+            raise ValueError(f"expected {self.params.ns} shots, got {acq.src.shape[0]}")
+        _native.check(self.lib.gb_fwi3d_validate(ctypes.byref(self.cp), ctypes.byref(acq.c)), "gb_fwi3d_validate")
+        self.acq = acq
+
     def _flags(self, forward_only: bool) -> int:
         return (FORWARD_ONLY if forward_only else 0) | (CHECKPOINT if self.checkpoint and not forward_only else 0)
 
@@ -286,16 +294,16 @@ class Posterior:
         self.checkpoint = checkpoint
         self._mask_dev = torch.as_tensor(self.mask, device=self.device)
         self._data_dev = torch.as_tensor(self.data, device=self.device)
-        self._engines = {}
+        self._eng = None
 
     def _engine(self, slices) -> Fwi3dEngine:
-        key = tuple(int(s) for s in slices)
-        if key not in self._engines:
-            if len(self._engines) > 8:
-                self._engines.clear()
-            self._engines[key] = Fwi3dEngine(self.params, self.shots[slices], self.rec, self.wavelet,
-                                             device=self.device, checkpoint=self.checkpoint)
-        return self._engines[key]
+        """One engine (and workspace) for every shot subset: only the sources change."""
+        if self._eng is None:
+            self._eng = Fwi3dEngine(self.params, self.shots[slices], self.rec, self.wavelet, device=self.device,
+                                    checkpoint=self.checkpoint)
+        else:
+            self._eng.set_sources(self.shots[slices])
+        return self._eng
 
     def fwi3d(self, x):
         """x (m, ndim) -> (0.5 * loss * scale (m,), grad * scale (m, ndim)) for a
