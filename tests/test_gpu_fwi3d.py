@@ -129,3 +129,12 @@ def test_posterior_drop_in(engine_lib, cuda, tmp_path):
     assert logp.is_cuda and x.grad.is_cuda
     assert np.allclose(-logp.detach().cpu().numpy() * 0.25, loss, rtol=1e-10)
     assert np.array_equal(x.grad.cpu().numpy(), -grad / 0.25)
+    # a second call draws another subset; the engine and its workspace are reused
+    np.random.seed(5)
+    sl2 = np.sort(np.random.choice(nshots, size=2, replace=False))
+    assert not np.array_equal(sl2, sl)
+    np.random.seed(5)
+    l2, g2 = post.fwi3d(x.detach())
+    ref2 = [O.run(sub, shots[sl2], c.rec, c.wav, v, data[sl2], grad=True) for v in full]
+    assert np.allclose(l2.cpu().numpy(), np.array([r[2] for r in ref2]) * scale, rtol=1e-10)
+    assert np.array_equal(g2.cpu().numpy(), np.stack([r[1][mask] for r in ref2]).astype(np.float64) * scale)
