@@ -379,7 +379,11 @@ __global__ void k_prepare(const Geom g, const float *__restrict__ vel, float *__
 
 // grad[s][cell] = sum over shots, in double, of the per-shot accumulated
 // sum(psave * p2), times the reference's per-term factor
-// -2/powf(v,3) * nt_interval * dt (FWI) or nt_interval * dt (imaging).
+// -2/powf(v,3) * nt_interval * dt (FWI) or nt_interval * dt (imaging).  In FWI
+// mode the stored field is p2 - 2 p1 + p0, not the reference's
+// (p2 - 2 p1 + p0)/dt/dt (backward_IO's psave, fdtd2D_modelling.c:902-939):
+// the 1/dt^2 is applied here, once per cell in FP64, instead of two
+// correctly rounded divisions per cell and stored step.
 __global__ void k_reduce_grad(const Geom g, const float *__restrict__ gacc,
                               const float *__restrict__ vel, float *__restrict__ grad,
                               int nsamples, int imaging)
@@ -399,7 +403,7 @@ __global__ void k_reduce_grad(const Geom g, const float *__restrict__ gacc,
         if (!imaging) {
             const double v = (double)vel[e];
             const float v3 = __double2float_rn(v * v * v);  // powf(v, 3) as a rounded float
-            coef = (-2.0 / (double)v3) * coef;
+            coef = (-2.0 / (double)v3) * coef / ((double)g.dt * (double)g.dt);
         }
         grad[e] = __double2float_rn(coef * acc);
     }

@@ -283,14 +283,9 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
     *p2 = q;
     if (ps) {
         if (!ADJ) {
-            float v = q;
-            if (!b.imaging) {
-                const float x = fa(fs(q, fm(2.0f, p1c)), p0c);
-                const bool okt = g.fast_dt && in_fast_range(x, kDiv2Lo, kDiv2Hi);
-                v = div2_fast(x, g.dt, -g.rdt);
-                if (!__all_sync(0xffffffffu, okt) && !okt) v = div2_any(x, g.dt, g.rdt, g.fast_dt);
-            }
-            *ps = v;
+            // FWI stores p2 - 2 p1 + p0; the 1/dt^2 of d2p/dt2 is applied once,
+            // in FP64, by the gradient reduction.
+            *ps = b.imaging ? q : fa(fs(q, fm(2.0f, p1c)), p0c);
         } else {
             *G = fa(gv, fm(psv, q));  // psv = *ps, gv = *G, loaded ahead
         }
@@ -468,7 +463,7 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
         if (w.ps && iz >= g.pml && iz < g.ntz - g.pml) {
             const long long pc = (long long)(iz - g.pml) * g.ipitch;
             if (!ADJ)
-                w.ps[pc] = b.imaging ? q : div2_any(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+                w.ps[pc] = b.imaging ? q : fa(fs(q, fm(2.0f, p1c)), p0c);
             else
                 w.G[pc] = fa(gv, fm(psv, q));
         }

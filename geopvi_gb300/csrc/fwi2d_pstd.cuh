@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256) k_step_pstd(const Geom g, const Batch b, 
         const long long pc = ((long long)slot * g.nt_save + sa.snap) * g.pstride + (long long)(iz - g.pml) * g.ipitch +
                              (ix - g.pml + g.ioff);
         if (!ADJ) {
-            b.psave[pc] = b.imaging ? q : div2_any(fa(fs(q, fm(2.0f, p1c)), p0c), g.dt, g.rdt, g.fast_dt);
+            b.psave[pc] = b.imaging ? q : fa(fs(q, fm(2.0f, p1c)), p0c);  // 1/dt^2 in the reduction
         } else {
             float *G = b.gacc + (long long)inst * g.pstride + (long long)(iz - g.pml) * g.ipitch + (ix - g.pml + g.ioff);
             *G = fa(*G, fm(b.psave[pc], q));
