@@ -237,10 +237,8 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     fd_weights(g.Lc, g.fd);
     g.rdx = 1.0f / p.dx;
     g.rdz = 1.0f / p.dz;
-    g.rdt = 1.0f / p.dt;
     g.fast_dx = division_is_exact(p.dx) ? 1 : 0;
     g.fast_dz = division_is_exact(p.dz) ? 1 : 0;
-    g.fast_dt = division_is_exact(p.dt) ? 1 : 0;
     ricker(p.nt, p.dt, p.f0, d.rik);
     g.pstd = p.laplace_solver == 1 ? 1 : 0;
     if (g.pstd) wavenumber(g.ntx, g.ntz, p.dx, p.dz, d.kk);

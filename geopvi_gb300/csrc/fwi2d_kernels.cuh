@@ -70,12 +70,12 @@ struct Geom {
     int ds, s_ix0;       // source column of shot is: s_ix0 + is*ds
     int ns, nt, nti, nt_save;
     int tiles_x, tiles_z;
-    int fast_dx, fast_dz, fast_dt;  // the host proved div_const exact for this divisor
+    int fast_dx, fast_dz;  // the host proved div_const exact for this divisor
     int pstd;            // laplace_solver = 1: pseudo-spectral Laplacian
     long long fstride;   // floats per padded field (ntz * pitch)
     long long pstride;   // floats per interior snapshot (nz * ipitch)
     float dx, dz, dt;
-    float rdx, rdz, rdt; // RN(1/dx), RN(1/dz), RN(1/dt)
+    float rdx, rdz;      // RN(1/dx), RN(1/dz)
     float fd[8];
 };
 
