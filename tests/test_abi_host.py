@@ -12,7 +12,7 @@ import pytest
 
 import cases
 from geopvi_gb300 import _native
-from geopvi_gb300.params import Params, prepare_fwi_parameters, read_paramfile, write_paramfile
+from geopvi_gb300.params import prepare_fwi_parameters, read_paramfile, write_paramfile
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
                       "geopvi_fwi2d.h")
