@@ -31,12 +31,12 @@ import torch
 from . import _native
 from .params import Params
 
-# Cost model of one step launch on GB300, fitted to measured launches of the
-# step kernel (profile_step, bench plain mode): t = LAUNCH_OVERHEAD_S +
-# padded cells / CELL_RATE (one cfg2 solve, 0.11 M cells: 29 us; 140 solves,
-# 15.8 M cells: 195 us; 1280 solves, 144 M cells: 1.44 ms).
-CELL_RATE = 1.0e11
-LAUNCH_OVERHEAD_S = 25e-6
+# Cost model of one time step of a wave on GB300, fitted to measured steps
+# (bench plain mode and the cfg2 bench, stored steps): t = LAUNCH_OVERHEAD_S +
+# padded cells / CELL_RATE (one cfg2 solve, 0.11 M cells: 22 us, latency-bound;
+# 183 solves, 20.6 M cells: 131 us).
+CELL_RATE = 1.6e11
+LAUNCH_OVERHEAD_S = 20e-6
 
 
 @dataclass
