@@ -76,6 +76,38 @@ def test_forward_only_matches(engine_lib, cuda):
     assert np.array_equal(r.syn.cpu().numpy(), syn_o) and r.grad is None
 
 
+def test_edge_geometries(engine_lib, cuda):
+    """One shot and one receiver at opposite model corners, a one-cell absorbing
+    strip, 10th order, stored steps every 3rd of a 101-step run (also
+    checkpointed), and every receiver of another case in one cell."""
+    p = fwi3d.Fwi3dParams(nx=9, ny=7, nz=8, nt=101, dt=1e-3, dx=10.0, dy=10.0, dz=10.0, pml0=1, Lc=5,
+                          nt_interval=3, ns=1, nr=1)
+    src, rec = np.array([[0, 0, 0]]), np.array([[8, 6, 7]])
+    wav = ricker(p.nt, p.dt, 25.0)
+    rng = np.random.default_rng(9)
+    truth = (1800 + 500 * rng.random(p.ncell)).astype(np.float32)
+    vel = (truth + rng.uniform(-80, 80, (2, p.ncell))).astype(np.float32)
+    obs = O.run(p, src, rec, wav, truth)[0]
+    outs = [O.run(p, src, rec, wav, v, obs, grad=True) for v in vel]
+    for ck in (False, True):
+        r = fwi3d.Fwi3dEngine(p, src, rec, wav, device=cuda, checkpoint=ck).run(
+            torch.from_numpy(vel).to(cuda), torch.from_numpy(obs).to(cuda), want_syn=True)
+        assert np.array_equal(r.syn.cpu().numpy(), np.stack([o[0] for o in outs]))
+        assert np.array_equal(r.grad.cpu().numpy(), np.stack([o[1] for o in outs]))
+        assert np.abs(outs[0][1]).max() > 0
+    # every receiver in one cell: injected one after another in receiver order
+    c = make_case(**CASES["o8"])
+    rec_same = np.repeat(c.rec[:1], 5, axis=0)
+    q = c.p.replace(nr=5)
+    obs5 = O.run(q, c.src, rec_same, c.wav, c.vel[0] * 0 + 1900)[0]
+    obs5 = obs5 + np.linspace(0, 1e-3, 5, dtype=np.float32)  # distinct residuals per receiver
+    ref = O.run(q, c.src, rec_same, c.wav, c.vel[0], obs5, grad=True)
+    r = fwi3d.Fwi3dEngine(q, c.src, rec_same, c.wav, device=cuda).run(
+        torch.from_numpy(c.vel[:1]).to(cuda), torch.from_numpy(np.ascontiguousarray(obs5)).to(cuda), want_syn=True)
+    assert np.array_equal(r.syn[0].cpu().numpy(), ref[0])
+    assert np.array_equal(r.grad[0].cpu().numpy(), ref[1])
+
+
 @pytest.mark.parametrize("checkpoint,resident", [(True, None), (False, 1), (True, 3)])
 def test_checkpoint_and_waves_identical(engine_lib, cuda, checkpoint, resident):
     c = make_case(**{**CASES["o8"], "nt": 150, "nsamples": 3})
