@@ -163,15 +163,28 @@ __global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const G
     // this plane's window value, p0 and v*dt, loaded one plane ahead
     float wn = z0 + H < g.ntz ? __ldg(p1 + (z0 + H) * g.sz + col) : 0.0f;
     float p0n = __ldg(p0 + z0 * g.sz + col), vdn = __ldg(vdc + z0 * g.sz);
+    // adjoint stored step: the stored field and the accumulator, also a plane ahead
+    float svn = 0.0f, gvn = 0.0f;
+    if (ADJ && sv && z0 >= g.pml && z0 < g.ntz - g.pml) {
+        const long long j = (long long)(z0 - g.pml) * ps;
+        svn = __ldg(sv + j);
+        gvn = Gv[j];
+    }
     GB_FWI3D_UNROLL(GB_FWI3D_ZUNROLL)
     for (int z = z0; z < z1; ++z) {
         win[2 * H] = wn;
         const float p0c = p0n, vd = vdn;
+        const float svc = svn, gvc = gvn;
         if (z + 1 < z1) {
             const int zn = z + 1 + H;
             wn = zn < g.ntz ? __ldg(p1 + zn * g.sz + col) : 0.0f;
             p0n = __ldg(p0 + (z + 1) * g.sz + col);
             vdn = __ldg(vdc + (z + 1) * g.sz);
+            if (ADJ && sv && z + 1 >= g.pml && z + 1 < g.ntz - g.pml) {
+                const long long j = (long long)(z + 1 - g.pml) * ps;
+                svn = __ldg(sv + j);
+                gvn = Gv[j];
+            }
         }
         const long long c = z * g.sz + col;
         float q = 0.0f;
@@ -223,7 +236,7 @@ __global__ void __launch_bounds__(kBX *kBY, GB_FWI3D_MIN_BLOCKS) k3_step(const G
                 if (!ADJ)
                     sv[j] = __fmul_rn(__fsub_rn(q, u), g.idt2);
                 else
-                    Gv[j] = fmaf_rn(__ldg(sv + j), q, Gv[j]);
+                    Gv[j] = fmaf_rn(svc, q, gvc);
             }
         }
         p2[c] = q;
