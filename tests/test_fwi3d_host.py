@@ -170,3 +170,31 @@ def test_file_helpers_round_trip(tmp_path):
     assert np.array_equal(np.load(tmp_path / "batch_data.npy"), data[sl])
     np.save(tmp_path / "pred.npy", data[sl] + 1)
     assert fwi3d.cal_loss(str(tmp_path / "pred.npy"), str(tmp_path / "batch_data.npy")) == pytest.approx(4 * 7 * 4)
+
+
+def test_posterior_reads_the_reference_config(tmp_path):
+    """Posterior(args, config, ...) takes the reference's [FWI] / [path] keys plus
+    dt (and optional pml, Lc, nt_interval); nt is the wavelet's length.  The
+    engine is created on the first call, so construction needs no GPU."""
+    import configparser
+    shots = np.array([[1, 2, 0], [3, 1, 1], [0, 0, 2]])
+    rec = np.array([[0, 0, 0], [2, 1, 0]])
+    wav = ricker(57, 1e-3, 20.0)
+    data = np.zeros((3, 57, 2), np.float32)
+    for name, arr in (("source", shots), ("data", data), ("rec", rec), ("wavelet", wav)):
+        np.save(tmp_path / f"{name}.npy", arr)
+    cfg = configparser.ConfigParser()
+    cfg["FWI"] = dict(nx="4", ny="3", nz="5", dx="10", dy="12", dz="9", dt="0.0008", shot_batch="2",
+                      vel_fixed="1500", recfile=str(tmp_path / "rec.npy"), waveletfile=str(tmp_path / "wavelet.npy"))
+    cfg["path"] = dict(inpath=str(tmp_path), outpath=str(tmp_path), srcfile=str(tmp_path / "source.npy"),
+                       datafile=str(tmp_path / "data.npy"))
+    post = fwi3d.Posterior(SimpleNamespace(sigma=0.3), cfg, device="cpu")
+    p = post.params
+    assert (p.nx, p.ny, p.nz, p.nt) == (4, 3, 5, 57) and p.dt == pytest.approx(0.0008)
+    assert (p.dx, p.dy, p.dz) == (10.0, 12.0, 9.0)
+    assert (p.pml0, p.Lc, p.nt_interval) == (10, 4, 1)  # defaults
+    assert post.mask.shape == (60,) and post.mask.all() and post.sigma == 0.3 and post.batch == 2
+    assert post.shots.shape == (3, 3) and post.rec.shape == (2, 3) and post.data.shape == (3, 57, 2)
+    cfg["FWI"].update(pml="6", Lc="5", nt_interval="3")
+    q = fwi3d.Posterior(SimpleNamespace(sigma=0.3), cfg, mask=np.arange(60) % 2 == 0, device="cpu").params
+    assert (q.pml0, q.Lc, q.nt_interval) == (6, 5, 3)
