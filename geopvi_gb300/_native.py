@@ -54,12 +54,20 @@ EXPORTED_SYMBOLS = (
     "gb_fwi2d_read_params", "gb_fwi2d_validate", "fwi_2D", "forward_2D",
     "gb_fwi2d_workspace_bytes", "gb_fwi2d_batch", "gb_fwi2d_last_launch_count",
     "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms", "gb_fwi2d_status",
-    "gb_fwi2d_batch_noalloc", "gb_fwi2d_tuned_variant",
+    "gb_fwi2d_batch_noalloc", "gb_fwi2d_tuned_variant", "gb_fwi2d_instances_workspace_bytes",
+    "gb_fwi2d_run_instances",
 )
 
 
 class CParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in INT_FIELDS] + [(n, ctypes.c_float) for n in FLOAT_FIELDS]
+
+
+class CInstance(ctypes.Structure):
+    """gb_fwi2d_instance: one entry of an uneven batch (device pointers)."""
+    _fields_ = [("params", CParams), ("nsamples", ctypes.c_int), ("vel", ctypes.c_void_p),
+                ("obs", ctypes.c_void_p), ("syn", ctypes.c_void_p), ("grad", ctypes.c_void_p),
+                ("misfit", ctypes.c_void_p)]
 
 
 class EngineError(RuntimeError):
@@ -113,6 +121,12 @@ def load() -> ctypes.CDLL:
         L.gb_fwi2d_status.restype = ctypes.c_int
         L.gb_fwi2d_tuned_variant.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_uint]
         L.gb_fwi2d_tuned_variant.restype = ctypes.c_int
+        I = ctypes.POINTER(CInstance)
+        L.gb_fwi2d_instances_workspace_bytes.argtypes = [I, ctypes.c_int, ctypes.c_int, ctypes.c_uint]
+        L.gb_fwi2d_instances_workspace_bytes.restype = ctypes.c_size_t
+        L.gb_fwi2d_run_instances.argtypes = [I, ctypes.c_int, ctypes.c_uint, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_size_t, ctypes.c_void_p]
+        L.gb_fwi2d_run_instances.restype = ctypes.c_int
         L.gb_fwi2d_release_caches.argtypes = []
         L.gb_fwi2d_release_caches.restype = None
         L.gb_fwi2d_version.argtypes = []

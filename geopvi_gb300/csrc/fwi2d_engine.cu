@@ -1400,6 +1400,52 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     return st;
 }
 
+size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, int max_resident,
+                                          unsigned flags)
+{
+    if (!inst || n <= 0) return 0;
+    size_t most = 0;
+    for (int i = 0; i < n; ++i) {
+        const size_t b = gb_fwi2d_workspace_bytes(&inst[i].params, inst[i].nsamples, max_resident, flags);
+        if (b == 0) return 0;
+        most = std::max(most, b);
+    }
+    return most;
+}
+
+int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
+                           void *work, size_t work_bytes, void *stream)
+{
+    t_last_launches = 0;
+    if (!inst || n <= 0 || !work) return GB_FWI2D_EINVAL;
+    const bool exact = (flags & GB_FWI2D_EXACT_GRADIENT) != 0;
+    if (exact && (flags & GB_FWI2D_IMAGING)) return GB_FWI2D_EINVAL;
+    if (((flags >> GB_FWI2D_VARIANT_SHIFT) & 0xFu) > (unsigned)kNumStepVariants) return GB_FWI2D_EINVAL;
+    for (int i = 0; i < n; ++i) {  // everything checked before anything is enqueued
+        const gb_fwi2d_instance &x = inst[i];
+        if (x.nsamples <= 0 || !x.vel || !x.obs || (!(flags & GB_FWI2D_FORWARD_ONLY) && !x.grad))
+            return GB_FWI2D_EINVAL;
+        const int st = gb_fwi2d_validate(&x.params);
+        if (st) return st;
+        if (exact && x.params.laplace_solver == 1 && !(flags & GB_FWI2D_FORWARD_ONLY)) return GB_FWI2D_ENOTSUP;
+        if (gb_fwi2d_workspace_bytes(&x.params, x.nsamples, max_resident, flags) > work_bytes)
+            return GB_FWI2D_ENOMEM;
+    }
+    long long launches = 0;
+    for (int i = 0; i < n; ++i) {
+        const gb_fwi2d_instance &x = inst[i];
+        const int st = gb_fwi2d_batch(&x.params, x.nsamples, x.vel, x.obs, x.syn, x.grad, x.misfit, flags,
+                                      max_resident, work, work_bytes, stream);
+        launches += t_last_launches;
+        if (st) {
+            t_last_launches = launches;
+            return st;
+        }
+    }
+    t_last_launches = launches;
+    return GB_FWI2D_OK;
+}
+
 long long gb_fwi2d_last_launch_count(void) { return t_last_launches; }
 
 int gb_fwi2d_tuned_variant(const gb_fwi2d_params *p, int nsamples, int max_resident, unsigned flags)

@@ -117,6 +117,34 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
                    float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
                    void *work, size_t work_bytes, void *stream);
 
+/* One entry of an uneven batch: its own parameter set (grid, shots, nt, f0
+ * ...), number of models and device buffers, laid out as in gb_fwi2d_batch. */
+typedef struct gb_fwi2d_instance {
+    gb_fwi2d_params params;
+    int nsamples;
+    const float *vel;   /* [nsamples][nz*nx] */
+    const float *obs;   /* [ns][nt][nr] */
+    float *syn;         /* [nsamples][ns][nt][nr], or NULL */
+    float *grad;        /* [nsamples][nz*nx], or NULL with GB_FWI2D_FORWARD_ONLY */
+    double *misfit;     /* [nsamples], or NULL */
+} gb_fwi2d_instance;
+
+/* Workspace for gb_fwi2d_run_instances: the largest instance's
+ * gb_fwi2d_workspace_bytes (the instances reuse one workspace in stream
+ * order); 0 if an instance is invalid. */
+size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, int max_resident,
+                                          unsigned flags);
+
+/* An uneven batch -- instances with different parameter sets -- on one
+ * stream, each through the gb_fwi2d_batch path, in order, on one shared
+ * workspace.  Every instance is checked before anything is enqueued: an
+ * invalid one returns its status (GB_FWI2D_EINVAL, GB_FWI2D_ENOMEM for a
+ * workspace too small for it) and nothing runs.  The per-instance
+ * descriptor form of the batched API; concurrency across streams and memory
+ * admission for mixed workloads are geopvi_gb300/scheduler.py's. */
+int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
+                           void *work, size_t work_bytes, void *stream);
+
 /* Allocation-free variant of gb_fwi2d_batch.  No counterpart in the
  * reference (whose solver allocates and frees its own buffers on every call).
  *

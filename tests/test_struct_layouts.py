@@ -53,3 +53,12 @@ def header_struct_pointer(header, name):
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", text, flags=re.S).group(1)
     return [re.search(r"\*\s*(\w+)\s*$", d.strip()).group(1) for d in body.split(";") if d.strip()]
+
+
+def test_instance_struct_matches_header():
+    text = open(os.path.join(INCLUDE, "geopvi_fwi2d.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = re.search(r"typedef struct gb_fwi2d_instance\s*\{(.*?)\}\s*gb_fwi2d_instance;", text, flags=re.S).group(1)
+    names = [re.search(r"(\w+)\s*$", d.strip()).group(1) for d in body.split(";") if d.strip()]
+    assert names == [f for f, _ in _native.CInstance._fields_]
+    assert _native.CInstance._fields_[0][1] is _native.CParams
