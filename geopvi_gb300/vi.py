@@ -237,8 +237,8 @@ class FlowsBasedDistribution(nn.Module):
 def _to_torch_sparse(m, device=None):
     m = sparse.coo_matrix(m)
     idx = torch.from_numpy(np.vstack([m.row, m.col]).astype(np.int64))
-    return torch.sparse_coo_tensor(idx, torch.from_numpy(m.data), m.shape, device=device,
-                                   check_invariants=True).coalesce()
+    with torch.sparse.check_sparse_tensor_invariants(True):  # checked here, global setting untouched
+        return torch.sparse_coo_tensor(idx, torch.from_numpy(m.data), m.shape, device=device).coalesce()
 
 
 def _smooth_logp(x, S):
