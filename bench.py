@@ -220,18 +220,23 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def load_traffic(p, nres_avg: float):
-    """DRAM bytes per step launch from the committed ncu summary, scaled to
-    this workload by padded cells per launch (traffic grows in proportion)."""
-    path = os.path.join(REPO, "profiles", "k_step_traffic.json")
+def traffic_per_cell(name: str = "k_step_traffic.json"):
+    """DRAM bytes per padded cell-update from a committed ncu summary, or None."""
+    path = os.path.join(REPO, "profiles", name)
     if not os.path.exists(path):
         return None
     try:
         t = json.load(open(path))
-        per_cell = float(t["dram_bytes_per_launch"]) / float(t["padded_cells_per_launch"])
-        return per_cell * p.ntp * nres_avg
+        return float(t["dram_bytes_per_launch"]) / float(t["padded_cells_per_launch"])
     except (KeyError, ValueError, ZeroDivisionError):
         return None
+
+
+def load_traffic(p, nres_avg: float):
+    """DRAM bytes per step launch from the committed ncu summary, scaled to
+    this workload by padded cells per launch (traffic grows in proportion)."""
+    per_cell = traffic_per_cell()
+    return None if per_cell is None else per_cell * p.ntp * nres_avg
 
 
 def run_gpu(args):
@@ -560,6 +565,8 @@ def run_fwi3d(args):
         os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg / (ms / 1e3) / 1e9
+    tpc = traffic_per_cell("k3_step_traffic.json")
+    traffic3 = None if tpc is None else tpc * ntp * resident
     # end to end through the Posterior: host float64 models in, numpy loss and gradient out
     e2e = None
     with tempfile.TemporaryDirectory() as d:
@@ -609,8 +616,10 @@ def run_fwi3d(args):
         "sample_gradients_per_s": nsamples * args.steps / (ms / 1e3),
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k3_step (3-D step) and its IO kernels, whole run",
-                     "algorithmic_bytes_per_step": alg / args.steps},
+                     "traffic": traffic3, "kernel": "k3_step (3-D step) and its IO kernels, whole run",
+                     "per": "time step of a wave: algorithmic and DRAM bytes of one step of the resident "
+                            "solves (DRAM scaled from profiles/k3_step_traffic.json by padded cells)",
+                     "algorithmic_bytes_per_launch": alg / (args.steps * 2 * p.nt * -(-(nsamples * p.ns) // resident))},
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
     }), flush=True)
 
