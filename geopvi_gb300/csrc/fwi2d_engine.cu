@@ -246,10 +246,7 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     d.blend_fp32 = true;
     for (int i = 0; i < p.pml0; ++i) {
         BlendCoef &c = d.coef[i];
-        c.w = (float)(1.0 - 1.0 * i / p.pml0);  // fdtd2D_modelling.c:229
-        c.omw = 1.0 - (double)c.w;
-        c.bh = (float)c.omw;
-        c.bl = (float)(c.omw - (double)c.bh);
+        blend_coef_init(c, i, p.pml0);  // w = 1 - i/pml0, fdtd2D_modelling.c:229
         // The FP32 blend needs bh + bl == 1 - w exactly and (1 - w) * q exact in
         // double for any float q: 1 - w may hold at most 53 - 24 = 29 significant bits.
         if ((double)c.bh + (double)c.bl != c.omw || significant_bits(c.omw) > 29) d.blend_fp32 = false;
@@ -444,6 +441,19 @@ __global__ void k_misfit_final(const double *__restrict__ part, double *__restri
     misfit[s] = 0.5 * acc;
 }
 
+// The boundary weights of derive() (w = 1 - i/pml0, fdtd2D_modelling.c:227-230,
+// the split of 1 - w and blend_fast's constants) built on the device, for
+// callers that must not copy from host memory.  blend_coef_init uses only
+// correctly rounded IEEE operations, so the table equals the host's bit for bit.
+__global__ void k_blend_coef(int pml0, BlendCoef *coef)
+{
+    for (int i = threadIdx.x; i < pml0; i += blockDim.x) {
+        BlendCoef c;
+        blend_coef_init(c, i, pml0);
+        coef[i] = c;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Cached per-device tables and graphs
 // ---------------------------------------------------------------------------
@@ -522,12 +532,33 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
+// Encoding a tensor map needs a current driver context, and a host thread
+// that has made no runtime call that binds one (cudaGetDevice and
+// cudaGetLastError do not) has none.  Bind the current device's primary
+// context then -- but leave a context the caller made current alone.
+static bool ensure_context()
+{
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+    });
+    CUcontext ctx = nullptr;
+    if (get_current && get_current(&ctx) == CUDA_SUCCESS && ctx) return true;
+    int dev = 0;
+    return cudaGetDevice(&dev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess;
+}
+
 // A 3-D fp32 tensor map over `depth` padded fields [depth][ntz][pitch] with a
 // (box_x, box_z, 1) box; out-of-range elements of a box read as zero.
 static bool make_map(CUtensorMap &m, void *base, const Geom &g, long long depth, int box_x, int box_z)
 {
     auto enc = tensor_map_encoder();
-    if (!enc) return false;
+    if (!enc || !ensure_context()) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ntz, (cuuint64_t)depth};
     const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.fstride * 4};
     const cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_z, 1};
@@ -773,6 +804,8 @@ struct Call {
     Maps maps2;  // checkpointing: the adjoint's ring
     const float *kk = nullptr;  // pseudo-spectral mode: |k|^2 table on the device
     int variant = 0;            // k_step variant (kStepVariants)
+    bool single_stream = false; // never fork onto the side stream (no stream or event is created)
+    bool clear_status = true;   // zero the status word first (false: keep an earlier call's flags)
     // Tuning: waves [0, trials.size()) run variant trials[i] between events
     // trial_ev[i]; later waves run `variant`.
     std::vector<int> trials;
@@ -923,7 +956,7 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     k_exact_tables<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.tab.coef, vdt, c.nsamples,
                                                                                    cells, abeta);
     launches += 2;
-    cudaMemsetAsync(status, 0, sizeof(int), st);
+    if (c.clear_status) cudaMemsetAsync(status, 0, sizeof(int), st);
     cudaMemsetAsync(gpad, 0, fbytes * ninst, st);
 
     Batch b{};
@@ -1034,7 +1067,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
     k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt,
                                                                                 c.nsamples);
     ++launches;
-    cudaMemsetAsync(status, 0, sizeof(int), st);
+    if (c.clear_status) cudaMemsetAsync(status, 0, sizeof(int), st);
     if (!fwd_only) cudaMemsetAsync(gacc, 0, sizeof(float) * g.pstride * ninst, st);
 
     Batch b;
@@ -1059,8 +1092,9 @@ static long long enqueue(const Call &c, cudaStream_t st)
     const int wave = plain ? 1 : c.L.resident;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(st, &cs);
-    const SideStream *side = (g.pstd || wave < kSplitMinResident) ? nullptr
-                                                                   : side_stream(cs == cudaStreamCaptureStatusNone);
+    const SideStream *side = (g.pstd || wave < kSplitMinResident || c.single_stream)
+                                 ? nullptr
+                                 : side_stream(cs == cudaStreamCaptureStatusNone);
     const bool ckpt = (c.flags & GB_FWI2D_CHECKPOINT) && !fwd_only;
     for (long long i0 = 0; i0 < ninst && ckpt; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
@@ -1328,12 +1362,16 @@ size_t gb_fwi2d_workspace_bytes(const gb_fwi2d_params *p, int nsamples, int max_
         .total;
 }
 
-int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
-                   float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
-                   void *work, size_t work_bytes, void *stream)
+// gb_fwi2d_batch's body.  clear_status false keeps the flags that earlier
+// work on the same workspace left in its status word (the instances of
+// gb_fwi2d_run_instances after the first).
+static int batch_impl(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs, float *syn,
+                      float *grad, double *misfit, unsigned flags, int max_resident, void *work,
+                      size_t work_bytes, void *stream, bool clear_status)
 {
     t_last_launches = 0;
     if (!p || nsamples <= 0 || !vel || !obs || !work) return GB_FWI2D_EINVAL;
+    cudaGetLastError();  // an earlier, unrelated error must not fail this call
     Derived d;
     int st = derive(*p, d);
     if (st) return st;
@@ -1355,6 +1393,7 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     c.flags = flags;
     c.work = (char *)work;
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
+    c.clear_status = clear_status;
     if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
         return GB_FWI2D_ECUDA;
     if (ckpt && !exact && !(flags & GB_FWI2D_FORWARD_ONLY) &&
@@ -1400,6 +1439,14 @@ int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, con
     return st;
 }
 
+int gb_fwi2d_batch(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
+                   float *syn, float *grad, double *misfit, unsigned flags, int max_resident,
+                   void *work, size_t work_bytes, void *stream)
+{
+    return batch_impl(p, nsamples, vel, obs, syn, grad, misfit, flags, max_resident, work, work_bytes, stream,
+                      true);
+}
+
 size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, int max_resident,
                                           unsigned flags)
 {
@@ -1434,8 +1481,10 @@ int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags,
     long long launches = 0;
     for (int i = 0; i < n; ++i) {
         const gb_fwi2d_instance &x = inst[i];
-        const int st = gb_fwi2d_batch(&x.params, x.nsamples, x.vel, x.obs, x.syn, x.grad, x.misfit, flags,
-                                      max_resident, work, work_bytes, stream);
+        // The status word is cleared by the first instance only, so a bounded
+        // wait that gave up in any instance stays visible to gb_fwi2d_status.
+        const int st = batch_impl(&x.params, x.nsamples, x.vel, x.obs, x.syn, x.grad, x.misfit, flags,
+                                  max_resident, work, work_bytes, stream, i == 0);
         launches += t_last_launches;
         if (st) {
             t_last_launches = launches;
@@ -1465,9 +1514,16 @@ int gb_fwi2d_tuned_variant(const gb_fwi2d_params *p, int nsamples, int max_resid
     return it->second.done ? it->second.best : -1;
 }
 
+static int static_scratch(void **out);
+
 int gb_fwi2d_status(const void *work, void *stream)
 {
-    if (!work) return GB_FWI2D_EINVAL;
+    if (!work) {  // the allocation-free entry point's workspace on the current device
+        void *base = nullptr;
+        const int st = static_scratch(&base);
+        if (st) return st;
+        work = base;
+    }
     int h = 0;
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemcpyAsync(&h, work, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -1492,6 +1548,12 @@ double gb_fwi2d_profile_step_ms(long long *launches)
     }
     t_profile.reset();
     return total;
+}
+
+int gb_fwi2d_side_stream_count(void)
+{
+    std::lock_guard<std::mutex> lk(g_side_mutex);
+    return (int)g_side.size();
 }
 
 void gb_fwi2d_release_caches(void)
@@ -1632,18 +1694,16 @@ int forward_2D(char input_file[200], float *vel_inner, float *record_syn, int ru
 // a fixed array that this library reserves on every GPU that loads it, for
 // the life of the process.
 // ---------------------------------------------------------------------------
-namespace {
-
 static __device__ __align__(256) unsigned char g_static_scratch[GB_FWI2D_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_static_mutex;
-void *g_static_addr[kMaxDevices] = {};
+static constexpr int kMaxDevices = 64;
+static std::mutex g_static_mutex;
+static void *g_static_addr[kMaxDevices] = {};
 
 // Device address of the static scratch array on the current device.  In host
 // code the array's name is only a host-side stand-in, so the address is
 // looked up once per device (with that device current) and cached.
-int static_scratch(void **out)
+static int static_scratch(void **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GB_FWI2D_ECUDA;
@@ -1657,34 +1717,39 @@ int static_scratch(void **out)
     return GB_FWI2D_OK;
 }
 
-}  // namespace
-
 extern "C" int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, const float *vel, const float *obs,
                                       float *syn, float *grad, double *misfit, unsigned flags, void *stream)
 {
     t_last_launches = 0;
     if (!p || nsamples <= 0 || !vel || !obs) return GB_FWI2D_EINVAL;
-    if (flags & ~(GB_FWI2D_IMAGING | GB_FWI2D_FORWARD_ONLY | GB_FWI2D_PLAIN)) return GB_FWI2D_EINVAL;
+    if (flags & ~(GB_FWI2D_IMAGING | GB_FWI2D_FORWARD_ONLY | GB_FWI2D_PLAIN | GB_FWI2D_CHECKPOINT))
+        return GB_FWI2D_EINVAL;
+    cudaGetLastError();  // an earlier, unrelated error must not fail this call
     Derived d;
     int st = derive(*p, d);
     if (st) return st;
     if (d.g.pstd) return GB_FWI2D_ENOTSUP;  // the transform library allocates its plans
     const bool fwd_only = (flags & GB_FWI2D_FORWARD_ONLY) != 0;
+    const bool ckpt = (flags & GB_FWI2D_CHECKPOINT) && !fwd_only;
+    // The workspace starts at the array's base (its status word first, where
+    // gb_fwi2d_status(NULL, ...) reads it); the weight table sits at the end.
     const size_t coef_bytes = align256(sizeof(BlendCoef) * d.coef.size());
-    const size_t cap = GB_FWI2D_STATIC_SCRATCH_BYTES;
+    const size_t cap = GB_FWI2D_STATIC_SCRATCH_BYTES - coef_bytes;
     // Largest resident count whose workspace fits beside the weight table.
     const long long ninst = (long long)nsamples * d.g.ns;
-    Layout L = plan_layout(d.g, nsamples, 1, syn == nullptr, fwd_only);
-    if (coef_bytes + L.total > cap) return GB_FWI2D_E2BIG;
+    auto layout = [&](long long resident) {
+        return plan_layout(d.g, nsamples, (int)resident, syn == nullptr, fwd_only, ckpt);
+    };
+    if (layout(1).total > cap) return GB_FWI2D_E2BIG;
     long long lo = 1, hi = ninst;
     while (lo < hi) {
         const long long mid = (lo + hi + 1) / 2;
-        if (coef_bytes + plan_layout(d.g, nsamples, (int)mid, syn == nullptr, fwd_only).total <= cap)
+        if (layout(mid).total <= cap)
             lo = mid;
         else
             hi = mid - 1;
     }
-    L = plan_layout(d.g, nsamples, (int)lo, syn == nullptr, fwd_only);
+    const Layout L = layout(lo);
     void *base = nullptr;
     st = static_scratch(&base);
     if (st) return st;
@@ -1699,16 +1764,18 @@ extern "C" int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, co
     c.grad = grad;
     c.misfit = misfit;
     c.flags = flags;
-    c.work = (char *)base + coef_bytes;
+    c.work = (char *)base;
     c.profile = false;
-    c.tab.coef = (BlendCoef *)base;
-    // The weight table is copied from pageable host memory: the copy returns
-    // once the data are staged, so the local table may go out of scope.
-    if (cudaMemcpyAsync(c.tab.coef, d.coef.data(), sizeof(BlendCoef) * d.coef.size(), cudaMemcpyHostToDevice,
-                        s) != cudaSuccess)
-        return GB_FWI2D_ECUDA;
+    c.single_stream = true;  // the two-halves schedule would create a side stream and events
+    c.tab.coef = (BlendCoef *)((char *)base + cap);
     if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident)) return GB_FWI2D_ECUDA;
-    const long long launches = enqueue(c, s);
+    if (ckpt && !make_maps(c.maps2, d.g, (float *)(c.work + L.ring2), L.resident)) return GB_FWI2D_ECUDA;
+    t_enqueue_error = 0;
+    // The weight table is built on the device: no host-to-device copy.
+    k_blend_coef<<<1, 32, 0, s>>>(d.g.pml0, c.tab.coef);
+    const long long launches = 1 + enqueue(c, s);
     t_last_launches = launches;
-    return cudaGetLastError() == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
+    st = cudaGetLastError() == cudaSuccess ? GB_FWI2D_OK : GB_FWI2D_ECUDA;
+    if (st == GB_FWI2D_OK && t_enqueue_error) st = t_enqueue_error;
+    return st;
 }

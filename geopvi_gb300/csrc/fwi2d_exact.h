@@ -217,12 +217,73 @@ GBX_HD float div2_any(float x, float y, float r, int fast)
 // Split of 1 - w into floats bh + bl (exact) for the boundary blend, with
 // omw = 1 - w in double.  The host precomputes one per boundary weight and
 // enables the FP32 path only when (1 - w) * q is exact in double for every
-// float q, i.e. 1 - w has at most 29 significant bits.
+// float q, i.e. 1 - w has at most 29 significant bits.  khi and klo are the
+// bounds of blend_fast's one-FMA path (blend_coef_init).
 struct BlendCoef {
     float w;
     float bh, bl;
+    float khi, klo;
     double omw;
 };
+
+#if defined(__CUDA_ARCH__)
+GBX_HD uint64_t gbx_dbits(double v) { return (uint64_t)__double_as_longlong(v); }
+#else
+GBX_HD uint64_t gbx_dbits(double v)
+{
+    uint64_t b;
+    std::memcpy(&b, &v, sizeof b);
+    return b;
+}
+#endif
+
+// 2^k as a float, -126 <= k <= 127.
+GBX_HD float gbx_pow2(int k) { return gbx_from_bits((uint32_t)(127 + k) << 23); }
+
+// Boundary weight i of pml0: w = 1 - i/pml0 in double stored as float
+// (fdtd2D_modelling.c:227-230), 1 - w in double and as floats bh + bl, and
+// the constants of blend_fast.  Every operation is a correctly rounded IEEE
+// operation, so host and device produce the same table.
+//
+// blend_fast's one-FMA path: when bl = 0, omw = bh = B * 2^lam with B odd of
+// kb bits.  For normal a, q (a float, q in [2^-60, 2^60]) with biased
+// exponents ea, eq, X = a + bh*q is an integer multiple of 2^(min(ea, lam+eq)
+// - 150) below 2^(max(ea, kb+lam+eq) - 125), so X is a double whenever
+// max(ea, kb+lam+eq) - min(ea, lam+eq) <= 28, i.e. kb - 28 <= ea - eq - lam
+// <= 28.  |a| < 2^(28+lam) |q| implies ea - eq <= 28 + lam, and
+// |a| >= 2^(kb-28+lam) |q| implies ea - eq >= kb - 28 + lam; a = 0 gives
+// X = bh*q (at most 48 bits).  X a double means RN_d(X) = X, so the
+// reference's RN_f(RN_d(X)) is RN_f(X): one FMA.  khi = 2^(28+lam) and
+// klo = 2^(kb-28+lam); bh = 0 (w = 1) always qualifies (khi = inf, klo = 0);
+// weights with bl != 0 never do (khi = 0).
+GBX_HD void blend_coef_init(BlendCoef &c, int i, int pml0)
+{
+    c.w = (float)(1.0 - 1.0 * i / pml0);
+    c.omw = 1.0 - (double)c.w;
+    c.bh = (float)c.omw;
+    c.bl = (float)(c.omw - (double)c.bh);
+    c.khi = 0.0f;
+    c.klo = 0.0f;
+    if (c.omw == 0.0) {
+        c.khi = gbx_from_bits(0x7F800000u);  // +inf
+    } else if (c.bl == 0.0f) {
+        const uint64_t b = gbx_dbits(c.omw);
+        const int e = (int)((b >> 52) & 0x7FF);  // omw is a normal double in (0, 1]
+        uint64_t m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+        int lam = e - 1075;
+        while (!(m & 1u)) {
+            m >>= 1;
+            ++lam;
+        }
+        int kb = 0;
+        while (m) {
+            m >>= 1;
+            ++kb;
+        }
+        c.khi = gbx_pow2(28 + lam);
+        c.klo = gbx_pow2(kb - 28 + lam);
+    }
+}
 
 // RN_f(RN_d(a + omw * q)) for a = RN_f(w * ext), computed in FP32.
 //   ph + pl = bh*q and qh + ql = bl*q exactly (FMA two-products);
@@ -294,6 +355,28 @@ GBX_HD bool blend_mix_fp32(float a, float q, const BlendCoef &c, float *out)
         }
     }
     return false;
+}
+
+GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok);
+
+// True when blend_fast's one-FMA path gives the reference's value (see
+// blend_coef_init); q = 0 always qualifies (X = a exactly).
+GBX_HD bool blend_fma_ok(float a, float q, float khi, float klo)
+{
+    const float aq = std::fabs(q), aa = std::fabs(a);
+    return (q == 0.0f) |
+           ((aq >= 0x1p-60f) & (aq <= 0x1p60f) & (aa < gbx_mul(aq, khi)) & ((aa >= gbx_mul(aq, klo)) | (a == 0.0f)));
+}
+
+// blend_mix by reference to a table entry, out of line: the kernels' rare path.
+GBX_COLD float blend_mix_at(float a, float q, const BlendCoef *c, int fp32_ok) { return blend_mix(a, q, *c, fp32_ok); }
+
+// RN_f(RN_d(a + (1 - w) q)): one FMA where blend_fma_ok proves it, blend_mix
+// otherwise.  bh, khi, klo are the entry's fields, held in registers by the caller.
+GBX_HD float blend_fast(float a, float q, float bh, float khi, float klo, const BlendCoef *c, int fp32_ok)
+{
+    if (blend_fma_ok(a, q, khi, klo)) return gbx_fma(bh, q, a);
+    return blend_mix_at(a, q, c, fp32_ok);
 }
 
 GBX_HD float blend_mix(float a, float q, const BlendCoef &c, int fp32_ok)

@@ -34,6 +34,7 @@ def main():
     ap.add_argument("--ns", type=int, default=None)
     ap.add_argument("--nt-interval", type=int, default=None,
                     help="store every n-th step (keeps the stored field small for multi-pass captures)")
+    ap.add_argument("--variant", type=int, default=None, help="force a step-kernel variant (default: the tuner)")
     args = ap.parse_args()
     w = getattr(workloads, args.config)()
     p = w.params.replace(nt=args.nt)
@@ -45,7 +46,7 @@ def main():
         p = p.replace(nt_interval=args.nt_interval)
     nsamples = max(1, -(-args.solves // p.ns))
     dev = torch.device("cuda:0")
-    eng = Fwi2dEngine(p, device=dev, graph=False, max_resident=nsamples * p.ns)
+    eng = Fwi2dEngine(p, device=dev, graph=False, max_resident=nsamples * p.ns, variant=args.variant)
     idx = np.arange(nsamples) % w.samples.shape[0]
     vel = torch.from_numpy(np.ascontiguousarray(w.samples[idx])).to(dev)
     obs = torch.zeros(p.data_len, dtype=torch.float32, device=dev)
@@ -54,7 +55,8 @@ def main():
     torch.cuda.synchronize()
     ms, launches = eng.step_profile()
     cells = p.ntp * nsamples * p.ns
-    print(json.dumps({"config": args.config, "nt": p.nt, "solves": nsamples * p.ns,
+    print(json.dumps({"config": args.config, "grid": [p.nz, p.nx], "variant": args.variant, "nt": p.nt,
+                      "solves": nsamples * p.ns,
                       "step_launches": launches, "step_ms": ms, "ms_per_launch": ms / max(launches, 1),
                       "padded_cells_per_wave": cells, "gcells_per_s": cells * 2 * p.nt * args.repeat / ms / 1e6}))
 

@@ -139,7 +139,8 @@ size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, 
  * stream, each through the gb_fwi2d_batch path, in order, on one shared
  * workspace.  Every instance is checked before anything is enqueued: an
  * invalid one returns its status (GB_FWI2D_EINVAL, GB_FWI2D_ENOMEM for a
- * workspace too small for it) and nothing runs.  The per-instance
+ * workspace too small for it) and nothing runs.  The workspace's status word
+ * (gb_fwi2d_status) collects the flags of every instance of the call.  The per-instance
  * descriptor form of the batched API; concurrency across streams and memory
  * admission for mixed workloads are geopvi_gb300/scheduler.py's. */
 int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
@@ -158,10 +159,16 @@ int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags,
  *
  * Inputs and outputs are the caller's device buffers, as in gb_fwi2d_batch
  * (syn may be NULL).  flags: GB_FWI2D_IMAGING, GB_FWI2D_FORWARD_ONLY,
- * GB_FWI2D_PLAIN only.  The batch is split into as many waves as the scratch
- * needs; a batch whose per-sample state alone (padded v*dt, gradient
- * accumulators, synthetic data when syn is NULL) plus one resident solve does
- * not fit returns GB_FWI2D_E2BIG.
+ * GB_FWI2D_PLAIN and GB_FWI2D_CHECKPOINT only; with CHECKPOINT a solve keeps
+ * ~sqrt(nt) wavefield pairs instead of its stored field, so a gradient batch
+ * of realistic size fits (a 120 x 250, nt 2000 solve: ~26 MB instead of
+ * ~250 MB).  The batch is split into as many waves as the scratch needs; a
+ * batch whose per-sample state alone (padded v*dt, gradient accumulators,
+ * synthetic data when syn is NULL) plus one resident solve does not fit
+ * returns GB_FWI2D_E2BIG.  All work runs on `stream` alone: no stream or
+ * event is created, and no host memory is copied (the boundary-weight table
+ * is built by a kernel).  gb_fwi2d_status(NULL, stream) reads the status
+ * word of the last call on the current device.
  *
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
@@ -175,8 +182,15 @@ int gb_fwi2d_batch_noalloc(const gb_fwi2d_params *p, int nsamples, const float *
 
 /* Waits for `stream`, then reads the device status word at the start of a
  * workspace used by gb_fwi2d_batch: GB_FWI2D_OK, or GB_FWI2D_ETIMEOUT if a
- * kernel's bounded wait for its staged tiles gave up (results invalid). */
+ * kernel's bounded wait for its staged tiles gave up (results invalid).
+ * work = NULL reads the status of gb_fwi2d_batch_noalloc on the current
+ * device. */
 int gb_fwi2d_status(const void *work, void *stream);
+
+/* Diagnostic: the number of auxiliary CUDA streams the library holds (one
+ * per device and host thread that ran gb_fwi2d_batch's two-stream schedule;
+ * released by gb_fwi2d_release_caches).  No counterpart in the reference. */
+int gb_fwi2d_side_stream_count(void);
 
 /* Number of kernel launches the last gb_fwi2d_batch call on this thread
  * enqueued (graph replays count the kernels inside the graph). */

@@ -216,4 +216,47 @@ long long harness_blend_mismatches(int pml0, long long trials, unsigned seed, lo
     return bad;
 }
 
+// blend_fast (one FMA where its exponent test proves the result, blend_mix
+// otherwise) against the double formula, on realistic blends (a near w*q),
+// cancellation, near-midpoint sums, zeros, tiny, huge and subnormal operands.
+// Returns mismatches; *fast counts the trials the FMA path settled.
+long long harness_blend_fast(int pml0, long long trials, unsigned seed, long long *fast)
+{
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    std::uniform_int_distribution<int> E(-70, 70);
+    long long bad = 0, nfast = 0;
+    for (int i = 0; i < pml0; ++i) {
+        BlendCoef c;
+        blend_coef_init(c, i, pml0);
+        const bool ok = ((double)c.bh + (double)c.bl) == c.omw;
+        for (long long t = 0; t < trials; ++t) {
+            float q = (float)(U(rng) * std::ldexp(1.0, E(rng)));
+            float ext = q * (float)(1.0 + 0.3 * U(rng));  // smooth field: extrapolation near the value
+            switch (t % 11) {
+            case 1: ext = (float)(U(rng) * std::ldexp(1.0, E(rng))); break;   // unrelated magnitudes
+            case 2: ext = (float)(-(c.omw * q) / (c.w > 0 ? c.w : 1.0f) * (1.0 + 1e-7 * U(rng))); break;  // cancellation
+            case 3: q = 0.0f; break;
+            case 4: ext = 0.0f; break;
+            case 5: q = std::ldexp(q, -80); ext = std::ldexp(ext, -80); break;  // tails
+            case 6: q = 1e-41f * (float)U(rng); break;  // subnormal
+            case 7: q = std::ldexp(q, 55); ext = std::ldexp(ext, 60); break;  // huge
+            default: break;
+            }
+            const float a = c.w * ext;
+            if (t % 11 == 8 && c.omw > 0) {  // sum near a float midpoint
+                const float target = (float)(U(rng) * 4.0);
+                const double mid = 0.5 * ((double)target + (double)std::nextafter(target, 10.0f));
+                q = (float)((mid - (double)a) / c.omw);
+            }
+            if (blend_fma_ok(a, q, c.khi, c.klo)) ++nfast;
+            const float got = blend_fast(a, q, c.bh, c.khi, c.klo, &c, ok ? 1 : 0);
+            const float want = ref_mix(a, c.omw, q);
+            if (std::memcmp(&got, &want, 4) != 0) ++bad;
+        }
+    }
+    if (fast) *fast = nfast;
+    return bad;
+}
+
 }  // extern "C"

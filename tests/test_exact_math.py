@@ -35,6 +35,9 @@ def harness(tmp_path_factory):
     L.harness_blend_mismatches.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
                                            ctypes.POINTER(ctypes.c_longlong)]
     L.harness_blend_mismatches.restype = ctypes.c_longlong
+    L.harness_blend_fast.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_uint,
+                                     ctypes.POINTER(ctypes.c_longlong)]
+    L.harness_blend_fast.restype = ctypes.c_longlong
     return L
 
 
@@ -79,3 +82,14 @@ def test_blend_exact_ties(harness, pml0):
 def test_blend_matches_double_formula(harness, pml0):
     fb = ctypes.c_longlong(0)
     assert harness.harness_blend_mismatches(pml0, 20000, 1234 + pml0, ctypes.byref(fb)) == 0
+
+
+@pytest.mark.parametrize("pml0", [1, 5, 8, 10, 20, 30])
+def test_blend_one_fma_path_matches_double_formula(harness, pml0):
+    """blend_fast: one FMA where the exponent-spread test proves that the exact sum is a
+    double (so the reference's double rounding is a single rounding), the exact FP32 /
+    FP64 blend otherwise; bit for bit against the double formula."""
+    fast = ctypes.c_longlong(0)
+    trials = 40000
+    assert harness.harness_blend_fast(pml0, trials, 77 + pml0, ctypes.byref(fast)) == 0
+    assert fast.value > 0

@@ -214,3 +214,31 @@ def test_full_geometry_two_shots(engine_lib, cuda, oracle, config):
     assert np.array_equal(out["syn"][0], syn_o)
     e = rel(out["grad"][0], grad_o)
     assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
+
+
+def test_batch_from_a_fresh_host_thread(engine_lib, cuda):
+    """A host thread that has made no CUDA call yet (no context bound) can run a batch:
+    the library binds the device's primary context before it encodes its tensor maps."""
+    import ctypes
+    import threading
+
+    z = np.load(os.path.join(GOLDEN, "fwi_o8.npz"))
+    p = cases.params_from_npz(z)
+    dev = torch.device("cuda:0")
+    vel = torch.from_numpy(np.ascontiguousarray(z["start"][None], dtype=np.float32)).to(dev)
+    obs = torch.from_numpy(np.ascontiguousarray(z["obs"], dtype=np.float32)).to(dev)
+    cp = p.c()
+    nbytes = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(cp), 1, 0, 0)
+    work = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    syn = torch.empty(p.data_len, dtype=torch.float32, device=dev)
+    grad = torch.empty(p.ncell, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize(dev)
+    out = []
+    t = threading.Thread(target=lambda: out.append(engine_lib.gb_fwi2d_batch(
+        ctypes.byref(cp), 1, vel.data_ptr(), obs.data_ptr(), syn.data_ptr(), grad.data_ptr(), None, 0, 0,
+        work.data_ptr(), nbytes, None)))
+    t.start()
+    t.join()
+    assert out == [0]
+    torch.cuda.synchronize(dev)
+    assert np.array_equal(syn.cpu().numpy(), z["syn"])
