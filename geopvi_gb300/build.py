@@ -52,7 +52,7 @@ def _stale() -> bool:
 
 
 def _defines() -> list[str]:
-    """Build-time tuning knobs, e.g. GEOPVI_GB300_DEFINES="GB_FWI2D_MIN_BLOCKS=8"."""
+    """Extra preprocessor definitions, e.g. GEOPVI_GB300_DEFINES="NAME=VALUE"."""
     return ["-D" + d for d in os.environ.get("GEOPVI_GB300_DEFINES", "").split() if d]
 
 

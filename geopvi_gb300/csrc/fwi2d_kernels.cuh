@@ -8,13 +8,16 @@
 // zero-lag imaging/gradient term (backward_IO, :941-978).  updata_p's copies
 // (:1053-1066) become a rotation of three buffers, so no step copies a field.
 //
-// Data movement: one block owns a 32-column x 64-row tile of one solve.  An
-// elected thread stages the previous time level with its stencil halo into
-// shared memory with one TMA tensor load completing on an mbarrier; each
-// warp then sweeps 16 rows of its 32 columns, keeping the z-stencil window in
+// Data movement: one block -- a single warp -- owns a 32-column x 16-row tile
+// of one solve.  An elected lane stages the previous time level with its
+// stencil halo into shared memory with one TMA tensor load completing on an
+// mbarrier; the warp then sweeps its 16 rows, keeping the z-stencil window in
 // registers, reading the level before (p0) and v*dt with coalesced loads, and
 // writes the new level, the stored snapshot (forward) or the gradient
-// accumulator (adjoint) with coalesced 128-byte row stores.
+// accumulator (adjoint) with coalesced 128-byte row stores.  One warp per
+// block lets a warp of cheap interior rows retire without waiting for a
+// slower absorbing-strip warp of the same tile (4-warp blocks of 64 rows
+// were 5 % slower on the 200 x 400 batch, 2-warp blocks no faster than 4).
 //
 // Arithmetic follows the reference operation by operation: __fmul_rn /
 // __fadd_rn / __fsub_rn never contract into FMA; divisions by the constant
@@ -34,30 +37,26 @@ namespace gbfwi {
 
 constexpr int kTileX = 32;    // columns per tile: one warp
 constexpr int kWarpRows = 16; // rows each warp sweeps
-constexpr int kWarps = 4;     // warps per block, stacked in z
-constexpr int kTileZ = kWarpRows * kWarps;  // 64 rows per tile
+constexpr int kWarps = 1;     // warps per block, stacked in z
+constexpr int kTileZ = kWarpRows * kWarps;  // 16 rows per tile
 constexpr int kHaloX = 8;     // x halo of the staged tiles (TMA x offsets stay 16-byte aligned)
 constexpr int kBoxX = kTileX + 2 * kHaloX;  // 48 staged columns
 constexpr int kThreads = kTileX * kWarps;   // 128
 
-// Resident blocks per SM the step kernel is compiled for (register cap
-// 65536 / (128 * this)); a build-time tuning knob.
 // Kernel variants: rows per block of the interior sweep (U; loads run one
-// block ahead) and resident blocks per SM the registers are capped for.  All
-// variants compute the same values bit for bit; the engine's tuner times them
-// on the caller's own batches and keeps the fastest per geometry and batch
-// shape.  (2, 8) is the default: on the cfg2 grid four rows overflow the
-// instruction cache (the unrolled row bodies carry inline exact fallbacks)
-// and fewer blocks per SM lose latency hiding.
+// block ahead) and resident blocks per SM the registers are capped for
+// (65536 / (32 * blocks) registers a thread).  All variants compute the same
+// values bit for bit; the engine's tuner times them on the caller's own
+// batches and keeps the fastest per geometry and batch shape.  (2, 32) is the
+// default: on the 200 x 400 grid four-row blocks overflow the instruction
+// cache (the unrolled row bodies carry inline exact fallbacks) and fewer
+// blocks per SM lose latency hiding.
 struct StepVariant {
     int rows, min_blocks;
 };
-constexpr StepVariant kStepVariants[] = {{2, 8}, {4, 8}, {1, 8}, {2, 6}};
+constexpr StepVariant kStepVariants[] = {{2, 32}, {4, 32}, {1, 32}, {2, 24}};
 constexpr int kNumStepVariants = sizeof(kStepVariants) / sizeof(kStepVariants[0]);
 
-#ifndef GB_FWI2D_MIN_BLOCKS
-#define GB_FWI2D_MIN_BLOCKS 8
-#endif
 
 // Geometry shared by every solve of one launch (one parameter set).
 struct Geom {
@@ -133,7 +132,11 @@ __device__ __forceinline__ float abc_blend(float q, float t11, float t12, float 
     ext = fs(ext, fm(fa(fm(t12, t12), fm(a2, t13)), p0c));
     ext = fs(ext, fm(fm(b2, t13), p0d));
     ext = fs(ext, fm(fm(t13, t13), p0e));
-    return blend_mix(fm(c.w, ext), q, c, fp32_ok);
+    // The double mix by one FMA where blend_fma_ok proves it (fwi2d_exact.h),
+    // the exact FP32 / FP64 evaluation otherwise.
+    const float a = fm(c.w, ext);
+    if (blend_fma_ok(a, q, c.khi, c.klo)) return __fmaf_rn(c.bh, q, a);
+    return blend_mix(a, q, c, fp32_ok);
 }
 
 // Receiver index of padded column ix on the receiver row, or -1.
@@ -242,7 +245,7 @@ __device__ __forceinline__ void laplacian_quotients(float lx, float lz, const Ge
 // Per-warp view of one step: where the warp's 16 x 32 cells live and which
 // buffers they read and write.
 struct WarpCtx {
-    const float *s1;             // staged p1 tile (48 columns x (64 + 2H) rows)
+    const float *s1;             // staged p1 tile (48 columns x (16 + 2H) rows)
     const float *p0;             // previous-previous level, padded field
     float *p2;                   // new level, padded field
     const float *vdt;            // v*dt, padded field
@@ -271,8 +274,11 @@ __device__ __forceinline__ void lean_row(const Geom &g, const Batch &b, const fl
         lx = fa(lx, fm(fd_weight<H>(m), fa(srow[m], srow[-m])));
         lz = fa(lz, fm(fd_weight<H>(m), fa(win[H + m], win[H - m])));
     }
-    const bool ok = (g.fast_dx & g.fast_dz) && in_fast_range(lx, kDiv2Lo, kDiv2Hi) &&
-                    in_fast_range(lz, kDiv2Lo, kDiv2Hi);
+    // div2_fast is proved for zero and 2^-80 <= |l| <= 2^80: both second
+    // differences within the range, or both zero (a field the wave has not
+    // reached); anything else takes div2_any below.
+    const float hi = fmaxf(fabsf(lx), fabsf(lz)), lo = fminf(fabsf(lx), fabsf(lz));
+    const bool ok = (g.fast_dx & g.fast_dz) && (hi <= kDiv2Hi) && ((lo >= kDiv2Lo) || (hi == 0.0f));
     float ddx = div2_fast(lx, g.dx, -g.rdx);
     float ddz = div2_fast(lz, g.dz, -g.rdz);
     if (!__all_sync(0xffffffffu, ok) && !ok) {
@@ -477,12 +483,12 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 
 // One time step of every solve in the wave, one block per (resident slot,
 // tile).  tm_p1 views the ring as [3*resident][ntz][pitch] with a
-// (48, 64+2H) box: the p1 tile and its halo are staged by one TMA load; p0
+// (48, 16+2H) box: the p1 tile and its halo are staged by one TMA load; p0
 // and v*dt are read once per cell with coalesced read-only loads (the
-// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~14 KB
-// per block.  Each warp then sweeps its 16 rows with the interior or the
+// boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~4.6 KB
+// per block.  The warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
-template <int H, bool ADJ, int U = 2, int MINB = GB_FWI2D_MIN_BLOCKS>
+template <int H, bool ADJ, int U, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
     k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
 {
