@@ -89,7 +89,8 @@ static int validate(const gb_fwi2d_params &p)
     if (p.laplace_solver != 0 && p.laplace_solver != 1) return GB_FWI2D_EINVAL;
     if (p.Lc < 3 || p.Lc > 6) return GB_FWI2D_EINVAL;     // fd_coefficient: Lc+1 in 4..7
     if (p.nr > 1 && p.dr == 0) return GB_FWI2D_EINVAL;    // receivers would share one cell
-    const long long Lc = p.Lc + 1, pml = p.pml0 + Lc;
+    // The pseudo-spectral mode sets Lc = 0 before pml = pml0 + Lc (fdtd2D_modelling.c:75-78).
+    const long long Lc = p.laplace_solver == 1 ? 0 : p.Lc + 1, pml = p.pml0 + Lc;
     const long long ntz = p.nz + 2 * pml, ntx = p.nx + 2 * pml;
     if (ntz > (1 << 20) || ntx > (1 << 20) || ntz * ntx > (1LL << 31)) return GB_FWI2D_EINVAL;
     const long long s_iz = pml + p.depths, r_iz = pml + p.depthr;
@@ -203,7 +204,10 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
     if (st) return st;
     Geom &g = d.g;
     std::memset(&g, 0, sizeof g);
-    g.Lc = p.Lc + 1;
+    // The pseudo-spectral Laplacian has no stencil halo: the reference sets
+    // Lc = 0 before pml = pml0 + Lc (fdtd2D_modelling.c:75-78), so its
+    // absorbing strips start at the grid's edge and there is no rim.
+    g.Lc = p.laplace_solver == 1 ? 0 : p.Lc + 1;
     g.pml = p.pml0 + g.Lc;
     g.pml0 = p.pml0;
     g.ntz = p.nz + 2 * g.pml;
@@ -1394,9 +1398,10 @@ static int batch_impl(const gb_fwi2d_params *p, int nsamples, const float *vel, 
     c.work = (char *)work;
     c.profile = (flags & GB_FWI2D_PROFILE) && !(flags & GB_FWI2D_GRAPH);
     c.clear_status = clear_status;
-    if (!make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
+    // The step kernel's tensor maps (the pseudo-spectral step reads the ring directly).
+    if (!d.g.pstd && !make_maps(c.maps, d.g, (float *)(c.work + L.ring), L.resident))
         return GB_FWI2D_ECUDA;
-    if (ckpt && !exact && !(flags & GB_FWI2D_FORWARD_ONLY) &&
+    if (ckpt && !exact && !d.g.pstd && !(flags & GB_FWI2D_FORWARD_ONLY) &&
         !make_maps(c.maps2, d.g, (float *)(c.work + L.ring2), L.resident))
         return GB_FWI2D_ECUDA;
     st = get_tables(d, c.tab);

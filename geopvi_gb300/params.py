@@ -64,10 +64,12 @@ class Params:
     dt: float = 1e-3
     f0: float = 10.0
 
-    # ---- derived sizes (fdtd2D_modelling.c:70, 85-89, 167-169) ----
+    # ---- derived sizes (fdtd2D_modelling.c:70, 75-78, 85-89, 167-169) ----
     @property
     def pml(self) -> int:
-        return self.pml0 + self.Lc + 1
+        # The pseudo-spectral Laplacian has no stencil halo: the reference sets
+        # Lc = 0 before pml = pml0 + Lc (fdtd2D_modelling.c:75-78).
+        return self.pml0 if self.laplace_solver == 1 else self.pml0 + self.Lc + 1
 
     @property
     def ntz(self) -> int:

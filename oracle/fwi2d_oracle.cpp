@@ -92,7 +92,10 @@ int make_geometry(const oracle_params &p, Geometry &g)
         return ORACLE_EINVAL;
     if (p.laplace_solver != 0 && p.laplace_solver != 1) return ORACLE_EINVAL;
     if (p.Lc < 3 || p.Lc > 6) return ORACLE_EINVAL;  /* fd_coefficient knows Lc+1 = 4..7 */
-    g.Lc = p.Lc + 1;
+    /* The pseudo-spectral Laplacian has no stencil halo: the reference sets
+     * Lc = 0 before pml = pml0 + Lc (fdtd2D_modelling.c:75-78, 85), so its
+     * absorbing strips start at the grid's edge. */
+    g.Lc = p.laplace_solver == 1 ? 0 : p.Lc + 1;
     g.pml = p.pml0 + g.Lc;
     g.ntz = p.nz + 2 * g.pml;
     g.ntx = p.nx + 2 * g.pml;

@@ -90,7 +90,8 @@ class Params:
 
     @property
     def pml(self) -> int:
-        return self.pml0 + self.Lc + 1
+        # pseudo-spectral mode: the reference sets Lc = 0 first (fdtd2D_modelling.c:75-78)
+        return self.pml0 if self.laplace_solver == 1 else self.pml0 + self.Lc + 1
 
     @property
     def data_len(self) -> int:
@@ -104,9 +105,18 @@ def write_paramfile(path: str, p: Params) -> None:
             f.write(f"{getattr(p, name)}\n")
 
 
+# Where this checkout keeps the reference solver's sources (read-only); the
+# GEOPVI_REFERENCE_FWI2D environment variable overrides it.  Absent on
+# machines that only hold this repository: the reference is then not built.
+REFERENCE_FWI2D = os.environ.get("GEOPVI_REFERENCE_FWI2D", "/root/reference/geopvi/forward/fwi2d")
+
+
 def build() -> None:
     """Compile the restatement (and the reference, if its sources exist)."""
-    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "all"], check=True)
+    cmd = ["make", "-s", "-C", ORACLE_DIR, "all"]
+    if os.path.isfile(os.path.join(REFERENCE_FWI2D, "fdtd2D_modelling.c")):
+        cmd.append(f"REF_SRC={REFERENCE_FWI2D}")
+    subprocess.run(cmd, check=True)
 
 
 _lib = None

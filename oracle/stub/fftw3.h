@@ -1,10 +1,9 @@
 /* Minimal FFTW3 declarations so the reference acoustic solver
  * (geopvi/forward/fwi2d/fdtd2D_modelling.c) compiles without FFTW.
  * Only the pseudo-spectral Laplacian (laplace_solver == 1,
- * fdtd2D_modelling.c:75-81 and :783-830) calls FFTW; the finite-difference
- * path that the oracle exercises never does.  The definitions in
- * fftw3_stub.c abort, so an accidental pseudo-spectral run fails loudly.
- * Test infrastructure only. */
+ * fdtd2D_modelling.c:75-81 and :783-830) calls FFTW.  fftw3_stub.c defines
+ * the seven calls it makes; its transform evaluates FFTW's definition of the
+ * unnormalised 2-D DFT directly.  Test infrastructure only. */
 #ifndef ORACLE_STUB_FFTW3_H
 #define ORACLE_STUB_FFTW3_H
 #include <stddef.h>

@@ -58,6 +58,26 @@ FULL = {
                                   dz=20.0, dt=0.002, f0=10.0), run_fwi=1, seed=21),
 }
 
+# Pseudo-spectral Laplacian (laplace_solver = 1): the reference's own
+# pstd_2d_calculate_p, with oracle/stub/fftw3_stub.c evaluating FFTW's
+# transform definition directly.  Every array is stored in full; these are
+# compared at tolerances, since two evaluations of the double transform
+# agree only to their last bits, which each step's float rounding amplifies.
+PSTD = {
+    # FWI gradient; the absorbing strips start at the grid's edge (pml = pml0)
+    "pstd_fwi": dict(params=Params(nx=40, nz=24, pml0=8, Lc=4, laplace_solver=1, ns=3, nt=260, ds=12, ns0=5,
+                                   depths=2, depthr=1, nr=36, dr=1, nr0=2, nt_interval=1, dx=10.0, dz=12.0,
+                                   dt=1e-3, f0=15.0), run_fwi=1, seed=31),
+    # imaging condition on odd padded sizes (45 x 41), stored every 2nd step
+    "pstd_img": dict(params=Params(nx=33, nz=29, pml0=6, Lc=3, laplace_solver=1, ns=2, nt=241, ds=15, ns0=3,
+                                   depths=3, depthr=0, nr=33, dr=1, nr0=0, nt_interval=2, dx=10.0, dz=10.0,
+                                   dt=1e-3, f0=20.0), run_fwi=0, seed=32),
+    # source and receivers inside the absorbing strip, sparse receivers
+    "pstd_ragged": dict(params=Params(nx=37, nz=19, pml0=5, Lc=4, laplace_solver=1, ns=2, nt=220, ds=30, ns0=-2,
+                                      depths=0, depthr=3, nr=11, dr=3, nr0=-3, nt_interval=1, dx=10.0, dz=10.0,
+                                      dt=1e-3, f0=18.0), run_fwi=1, seed=33),
+}
+
 SUBSAMPLE_TRACES = 10  # keep every 10th receiver of shot 0 in the full-size fixtures
 
 

@@ -1,9 +1,10 @@
 """Generate the golden fixtures from the reference solver itself.
 
 The reference's geopvi/forward/fwi2d/fdtd2D_modelling.c is compiled,
-unmodified, by ``make -C oracle ref`` into oracle/_ref/libref_fwi2d.so (with a
-stub fftw3.h; its finite-difference path never calls FFTW) and driven through
-its own entry points fwi_2D / forward_2D, the way the Cython module aco2d does
+unmodified, by oracle.build() into oracle/_ref/libref_fwi2d.so (with
+oracle/stub's FFTW stand-ins, whose transform evaluates FFTW's definition of
+the 2-D DFT directly, for the pseudo-spectral cases) and driven through its
+own entry points fwi_2D / forward_2D, the way the Cython module aco2d does
 (pyacofwi2D.pyx: float64 velocity cast to float32, zeroed outputs).
 
     python tests/golden/make_golden.py            # all cases
@@ -44,7 +45,7 @@ def sha(a: np.ndarray) -> str:
 
 
 def make_small(name: str) -> None:
-    c = cases.SMALL[name]
+    c = cases.SMALL[name] if name in cases.SMALL else cases.PSTD[name]
     p = c["params"]
     op = to_oracle(p)
     truth, start = cases.small_models(p, c["seed"])
@@ -77,8 +78,8 @@ def main(names):
         O.build()
     if not O.ref_available():
         raise SystemExit("reference solver not built: are the reference sources present?")
-    for n in names or list(cases.SMALL) + list(cases.FULL):
-        (make_small if n in cases.SMALL else make_full)(n)
+    for n in names or list(cases.SMALL) + list(cases.PSTD) + list(cases.FULL):
+        (make_full if n in cases.FULL else make_small)(n)
 
 
 if __name__ == "__main__":

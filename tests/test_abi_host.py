@@ -142,9 +142,12 @@ def test_batch_rejects_bad_arguments_without_gpu(engine_lib):
 
 def test_pseudo_spectral_workspace(engine_lib):
     """laplace_solver = 1 adds one dense complex-double transform array per resident solve."""
-    p = cases.SMALL["fwi_o8"]["params"]
-    fd = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.c()), 2, 3, 0)
-    ps = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.replace(laplace_solver=1).c()), 2, 3, 0)
+    p = cases.SMALL["fwi_o8"]["params"].replace(laplace_solver=1)
+    assert p.pml == p.pml0  # no stencil halo in this mode (fdtd2D_modelling.c:75-78)
+    same_grid = p.replace(laplace_solver=0, pml0=p.pml0 - (p.Lc + 1))  # the FD mode on the same padded grid
+    assert same_grid.ntp == p.ntp
+    fd = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(same_grid.c()), 2, 3, 0)
+    ps = engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.c()), 2, 3, 0)
     assert ps - fd >= 16 * p.ntp * 3
 
 

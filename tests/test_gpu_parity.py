@@ -216,6 +216,28 @@ def test_full_geometry_two_shots(engine_lib, cuda, oracle, config):
     assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
 
 
+@pytest.mark.slow
+def test_uneven_batch_largest_shape_two_shots(engine_lib, cuda, oracle):
+    """The largest shape of the uneven batch (400x800 grid, nt 5000, 5 Hz Ricker) on two
+    shots: forward data and synthetic data bit for bit against the FP32 oracle, gradient
+    within the bar."""
+    from geopvi_gb300 import workloads
+    p = workloads.make_params(400, 800, 5000, 1e-3, 2, 5.0)
+    rng = np.random.default_rng(44)
+    truth = workloads.layered(p.nz, p.nx, p.dx, rng).astype(np.float32).ravel()
+    start = (workloads.smooth(truth.reshape(p.nz, p.nx), passes=4, half=6).ravel()
+             + rng.uniform(-100.0, 100.0, p.ncell)).astype(np.float32)
+    op = oracle.Params(**cases.params_to_dict(p))
+    obs_o = oracle.forward_f32(op, truth)
+    fwd = run(engine_for(p, graph=False), truth, np.zeros(p.data_len, np.float32), forward_only=True)
+    assert np.array_equal(fwd["syn"][0], obs_o)
+    syn_o, grad_o = oracle.fwi_f32(op, start, obs_o, 1)
+    out = run(engine_for(p, graph=False), start, obs_o, want_syn=True)
+    assert np.array_equal(out["syn"][0], syn_o)
+    e = rel(out["grad"][0], grad_o)
+    assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
+
+
 def test_batch_from_a_fresh_host_thread(engine_lib, cuda):
     """A host thread that has made no CUDA call yet (no context bound) can run a batch:
     the library binds the device's primary context before it encodes its tensor maps."""

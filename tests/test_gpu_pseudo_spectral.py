@@ -7,8 +7,10 @@ That spread is intrinsic: two oracle builds differing only in the DFT's
 summation order (plain vs compensated) differ by 2.7-4.4e-6 on these cases,
 the FP32 and FP64 schemes by 3-5e-6, and the engine lands 1.9-8.2e-6 from
 the oracle.  Bars: synthetic data relative L2 <= 1e-5, gradient <= 1e-4
-(the tolerances stated for this path), misfit <= 1e-5.  Parity with the
-reference itself is unpinned (its FFTW path cannot be built here).
+(the tolerances stated for this path), misfit <= 1e-5.  The same bars hold
+against the reference's own pseudo-spectral code (fixtures pstd_*.npz, made by
+running fdtd2D_modelling.c with FFTW stand-ins that evaluate the transform's
+definition directly; tests/golden/make_golden.py).
 """
 import os
 
@@ -74,6 +76,26 @@ def test_pseudo_spectral_against_oracle(engine_lib, cuda, oracle, name):
     if not imaging:
         r = (syn_o - obs_o).astype(np.float64)
         assert abs(out["misfit"][0] - 0.5 * np.sum(r * r)) <= DATA_TOL * 0.5 * np.sum(r * r)
+
+
+@pytest.mark.parametrize("name", sorted(cases.PSTD))
+def test_pseudo_spectral_against_reference(engine_lib, cuda, name):
+    """The engine against the reference's own pstd_2d_calculate_p (fixtures pstd_*.npz):
+    forward data, synthetic data, gradient and misfit at the path's tolerances."""
+    z = load(name)
+    p = cases.params_from_npz(z)
+    assert p.laplace_solver == 1
+    imaging = int(z["run_fwi"]) == 0
+    fwd = run(p, z["truth"], np.zeros(p.data_len, np.float32), forward_only=True)
+    e = rel(fwd["syn"][0], z["obs"])
+    assert e <= DATA_TOL, f"forward data rel L2 {e:.3e}"
+    out = run(p, z["start"], z["obs"], imaging=imaging, want_syn=True)
+    e = rel(out["syn"][0], z["syn"])
+    assert e <= DATA_TOL, f"synthetic data rel L2 {e:.3e}"
+    e = rel(out["grad"][0], z["grad"])
+    assert e <= GRAD_TOL, f"gradient rel L2 {e:.3e}"
+    m = float(z["misfit"])
+    assert abs(out["misfit"][0] - m) <= DATA_TOL * abs(m)
 
 
 def test_pseudo_spectral_waves_plain_checkpoint(engine_lib, cuda, oracle):

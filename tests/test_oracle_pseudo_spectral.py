@@ -2,17 +2,44 @@
 
 pstd_2d_calculate_p (fdtd2D_modelling.c:783-830) transforms the padded field
 with FFTW in double, multiplies by -|k|^2 (wavenumber, :1127-1184) and
-transforms back.  FFTW is absent here, so the reference's pseudo-spectral
-path cannot be compiled: the restatement (a direct separable DFT) is checked
-against the mathematics instead -- exact on a plane wave up to the float
-rounding of |k|^2, equal to numpy's FFT to double round-off -- and the GPU
-engine is checked against the restatement (test_gpu_pseudo_spectral.py).
-Parity of this mode with the reference itself is unpinned.
+transforms back; in this mode the reference sets Lc = 0, so its absorbing
+strips start at the grid's edge (pml = pml0, :75-78).  The restatement (a
+direct separable DFT in double) is checked against the mathematics -- exact on
+a plane wave up to the float rounding of |k|^2, equal to numpy's FFT to double
+round-off -- and against the reference's own pseudo-spectral code, run with
+FFTW stand-ins that evaluate the transform's definition directly
+(oracle/stub/fftw3_stub.c; fixtures pstd_*.npz by tests/golden/make_golden.py).
+Two evaluations of the double transform agree only to their last bits, which
+every step's float rounding amplifies, so the fixtures are met at the path's
+stated tolerances: synthetic data relative L2 <= 1e-5, gradient <= 1e-4.
 """
+import os
+
 import numpy as np
 import pytest
 
 import cases
+
+GOLDEN = os.path.dirname(cases.__file__)
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("name", sorted(cases.PSTD))
+def test_restatement_against_reference_pseudo_spectral(oracle, name):
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    p = cases.params_from_npz(z)
+    assert p.laplace_solver == 1 and p.pml == p.pml0
+    op = oparams(oracle, p)
+    obs = oracle.forward_f32(op, z["truth"])
+    assert rel(obs, z["obs"]) <= 1e-5
+    syn, grad = oracle.fwi_f32(op, z["start"], z["obs"], int(z["run_fwi"]))
+    assert rel(syn, z["syn"]) <= 1e-5
+    assert rel(grad, z["grad"]) <= 1e-4
 
 
 def oparams(O, p):
