@@ -52,7 +52,8 @@ def parse_args():
                          "(each its own JSON line)")
     ap.add_argument("--requests", type=int, default=12, help="cfg5: requests served")
     ap.add_argument("--rate", type=float, default=200.0, help="cfg5: mean Poisson arrival rate (req/s)")
-    ap.add_argument("--cpu-shots", type=int, default=2, help="shots in the bounded CPU sample")
+    ap.add_argument("--cpu-shots", type=int, default=4, help="shots per sample in the bounded CPU sample")
+    ap.add_argument("--cpu-samples", type=int, default=3, help="samples timed in the CPU baseline (median reported)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -179,6 +180,19 @@ def cpu_sample(p, vel: np.ndarray, obs_shots: np.ndarray, shots: int):
     return cu / dt, dt, kind, O.get_threads(), desc
 
 
+def cpu_baseline(p, samples: np.ndarray, obs: np.ndarray, shots: int, nsamples: int) -> dict:
+    """The CPU baseline line: `nsamples` samples of `shots` shots each, timed
+    one after another; the median rate is reported with the spread."""
+    runs = [cpu_sample(p, samples[i % len(samples)], obs, shots) for i in range(nsamples)]
+    rates = [r[0] for r in runs]
+    v = float(statistics.median(rates))
+    kind, threads, desc = runs[0][2], runs[0][3], runs[0][4]
+    desc = desc.replace("1 sample x", f"median of {nsamples} samples x", 1)
+    return {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind, "sample": desc,
+            "seconds": float(sum(r[1] for r in runs)), "spread": [float(min(rates)), float(max(rates))],
+            "sample_gradients_per_s": v / cell_updates_per_sample(p)}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -201,8 +215,8 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append((v, dt))
         info = (kind, threads, desc)
-    value = float(np.mean([v for v, _ in vals]))
-    ms = float(np.mean([dt for _, dt in vals]) * 1e3)
+    value = float(statistics.median([v for v, _ in vals]))  # steps are single samples: the median is steadier
+    ms = float(statistics.median([dt for _, dt in vals]) * 1e3)
     kind, threads, desc = info
     out = {
         "impl": "reference", "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": value,
@@ -237,6 +251,25 @@ def load_traffic(p, nres_avg: float):
     this workload by padded cells per launch (traffic grows in proportion)."""
     per_cell = traffic_per_cell()
     return None if per_cell is None else per_cell * p.ntp * nres_avg
+
+
+def fwi_config(p):
+    """The example's [FWI] config section (config.ini keys) for a parameter set."""
+    import configparser
+    cfg = configparser.ConfigParser()
+    cfg["FWI"] = {"nx": str(p.nx), "nz": str(p.nz), "pml": str(p.pml0), "Lc": str(p.Lc),
+                  "laplace_slover": str(p.laplace_solver), "ns": str(p.ns), "nt": str(p.nt), "ds": str(p.ds),
+                  "ns0": str(p.ns0), "depths": str(p.depths), "depthr": str(p.depthr), "nr": str(p.nr),
+                  "dr": str(p.dr), "nr0": str(p.nr0), "nt_interval": str(p.nt_interval), "dx": repr(p.dx),
+                  "dz": repr(p.dz), "dt": repr(p.dt), "f0": repr(p.f0)}
+    return cfg
+
+
+def peak_hbm():
+    """(GB/s, 'measured' | 'fallback') from MEASURED_PEAKS.json."""
+    pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    peaks = json.load(open(pk_path)) if os.path.exists(pk_path) else {}
+    return float(peaks.get("hbm_gbs", 6800.0)), ("measured" if "hbm_gbs" in peaks else "fallback")
 
 
 def run_gpu(args):
@@ -295,12 +328,7 @@ def run_gpu(args):
     # roofline of the time-step kernel
     alg_total = algorithmic_bytes_per_sample(p) * nsamples * args.steps
     achieved = alg_total / (step_ms / 1e3) / 1e9
-    peaks = {}
-    pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
-    if os.path.exists(pk_path):
-        peaks = json.load(open(pk_path))
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    peak, peak_src = peak_hbm()
     # step_launches counts time steps of a wave; a wave of many resident
     # solves runs each step as two concurrent launches (one per half of the
     # solves, on two streams), so the per-step figures cover both.
@@ -338,14 +366,8 @@ def run_gpu(args):
     # end to end through the public Posterior.fwi: host float64 samples in, host loss/grad out
     e2e = None
     if not args.no_e2e:
-        import configparser
         from geopvi_gb300.posterior import Posterior
-        cfg = configparser.ConfigParser()
-        cfg["FWI"] = {"nx": str(p.nx), "nz": str(p.nz), "pml": str(p.pml0), "Lc": str(p.Lc),
-                      "laplace_slover": "0", "ns": str(p.ns), "nt": str(p.nt), "ds": str(p.ds),
-                      "ns0": str(p.ns0), "depths": str(p.depths), "depthr": str(p.depthr), "nr": str(p.nr),
-                      "dr": str(p.dr), "nr0": str(p.nr0), "nt_interval": str(p.nt_interval), "dx": repr(p.dx),
-                      "dz": repr(p.dz), "dt": repr(p.dt), "f0": repr(p.f0)}
+        cfg = fwi_config(p)
         del eng
         torch.cuda.empty_cache()
         with tempfile.TemporaryDirectory() as td:
@@ -367,9 +389,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, kind, threads, desc = cpu_sample(p, w.samples[0], obs.cpu().numpy(), args.cpu_shots)
-        cpu = {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind, "sample": desc,
-               "seconds": dt, "sample_gradients_per_s": v / cell_updates_per_sample(p)}
+        cpu = cpu_baseline(p, w.samples, obs.cpu().numpy(), args.cpu_shots, args.cpu_samples)
 
     if rank == 0:
         out = {
@@ -392,6 +412,141 @@ def run_gpu(args):
         }
         print(json.dumps(out), flush=True)
     grp.close()
+
+
+# ---------------------------------------------------------------------------
+# cfg3: the autograd path with sqrt(nt) checkpoints
+# ---------------------------------------------------------------------------
+def run_autograd(args):
+    """cfg3: log_prob = uniform prior + L2 likelihood through ForwardModel, the
+    forward state kept every ~sqrt(nt) steps and each segment recomputed in
+    the adjoint.  value: device-resident engine runs (useful cell-updates;
+    the recomputed steps are not counted); e2e: Posterior.log_prob(x) ->
+    .sum().backward() with host float64 samples in and the host gradient out."""
+    import torch
+    from geopvi_gb300 import vi
+    from geopvi_gb300.engine import Fwi2dEngine
+    from geopvi_gb300.posterior import Posterior
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    w = workload("cfg3", args.nt)
+    p = w.params
+    nsamples = w.samples.shape[0]
+    eng = Fwi2dEngine(p, device=dev, graph=False, checkpoint=True)
+    zeros = torch.zeros(p.data_len, dtype=torch.float32, device=dev)
+    obs = eng.run(torch.from_numpy(w.truth).to(dev).unsqueeze(0), zeros, forward_only=True).syn[0].clone()
+    sigma = 0.01 * float(obs.abs().max())  # noise: 1 % of the largest trace amplitude
+    vel = torch.from_numpy(w.samples).to(dev)
+
+    def timed(engine, v, steps, warmup, profile=False):
+        for _ in range(warmup):
+            engine.run(v, obs, profile=profile)
+        torch.cuda.synchronize(dev)
+        if profile and warmup:
+            engine.step_profile()  # discard the warm-up spans
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        e0.record()
+        for _ in range(steps):
+            launches += engine.run(v, obs, profile=profile).launches
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1), launches
+
+    for _ in range(args.warmup):
+        eng.run(vel, obs, profile=True)
+    torch.cuda.synchronize(dev)
+    eng.step_profile()
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    ms, launches = timed(eng, vel, args.steps, 0, profile=True)
+    clocks = sampler.stop()
+    step_ms, step_launches = eng.step_profile()
+    resident = eng._resident
+    cu_batch = cell_updates_per_sample(p) * nsamples
+    value = args.steps * cu_batch / (ms / 1e3)
+    # roofline of the step kernel over every launched step (forward, recomputed forward, adjoint)
+    alg = nsamples * p.ns * (3 * p.nt * 16 * p.ntp + p.nt_save * 16 * p.ncell) * args.steps
+    peak, peak_src = peak_hbm()
+    achieved = alg / (step_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": load_traffic(p, nsamples * p.ns * 3 * p.nt * args.steps / max(step_launches, 1)),
+                "peak_source": peak_src, "kernel": "k_step (fused FD step)",
+                "avg_launch_ms": step_ms / max(step_launches, 1), "step_share_of_region": step_ms / ms,
+                "algorithmic_bytes_per_launch": alg / max(step_launches, 1),
+                "per": "time step of a wave (forward, recomputed forward and adjoint steps alike)"}
+    del eng
+    torch.cuda.empty_cache()
+
+    # checkpoint overhead on a resident subset: 8 shots x 2 samples, one wave, both storage modes
+    sub = p.replace(ns=8)
+    sub_obs = obs.view(p.ns, p.nt, p.nr)[:8].contiguous().view(-1)
+    over = {}
+    for ck in (False, True):
+        e = Fwi2dEngine(sub, device=dev, graph=False, checkpoint=ck, max_resident=16)
+        for _ in range(2):
+            e.run(vel[:2], sub_obs)
+        torch.cuda.synchronize(dev)
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record()
+        e.run(vel[:2], sub_obs)
+        q1.record()
+        torch.cuda.synchronize(dev)
+        over["checkpoint" if ck else "full"] = q0.elapsed_time(q1)
+        del e
+        torch.cuda.empty_cache()
+    overhead = {"subset": "2 samples x 8 shots, 16 solves resident in one wave", "full_storage_ms": over["full"],
+                "checkpointed_ms": over["checkpoint"], "ratio": over["checkpoint"] / over["full"]}
+
+    # plain comparator: one (sample, shot) per launch, one sample
+    pe = Fwi2dEngine(p, device=dev, graph=False, plain=True)
+    pe.run(vel[:1], obs)
+    pms, _ = timed(pe, vel[:1], 1, 0)
+    plain = {"sample_gradients_per_s": 1e3 / pms, "cell_updates_per_s": cell_updates_per_sample(p) / (pms / 1e3),
+             "ms_per_sample": pms}
+    del pe
+    torch.cuda.empty_cache()
+
+    # end to end through autograd: host float64 samples in, host gradient out
+    with tempfile.TemporaryDirectory() as td:
+        prior = vi.Uniform(lower=np.full(p.ncell, 1400.0), upper=np.full(p.ncell, 5000.0))
+        post = Posterior(obs.cpu().numpy(), fwi_config(p), sigma=sigma, log_prior=prior.log_prob,
+                         paramfile=os.path.join(td, "p.txt"), device=dev, graph=False, checkpoint=True)
+        x = torch.from_numpy(w.samples.astype(np.float64)).requires_grad_(True)
+        for _ in range(2):
+            x.grad = None
+            post.log_prob(x).sum().backward()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            x.grad = None
+            logp = post.log_prob(x)
+            logp.sum().backward()
+            g = x.grad.numpy()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": args.steps * cu_batch / e2e_s, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": int(x.numel() * 8), "d2h_bytes_per_step": int(g.nbytes + logp.numel() * 8),
+               "api": "Posterior.log_prob(x).sum().backward() (host float64 samples in, host x.grad out)",
+               "sample_gradients_per_s": args.steps * nsamples / e2e_s}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(p, w.samples, obs.cpu().numpy(), args.cpu_shots, args.cpu_samples)
+    sgrad = args.steps * nsamples / (ms / 1e3)
+    print(json.dumps({
+        "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": value, "unit": "cell-updates/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded models)",
+        "config": {"workload": WORKLOAD_NAMES["cfg3"] + (f" (nt shortened to {p.nt})" if args.nt else ""),
+                   "samples": nsamples, "shots": p.ns, "grid": f"{p.nz}x{p.nx} (padded {p.ntz}x{p.ntx})",
+                   "nt": p.nt, "storage": "sqrt(nt) checkpoints, segments recomputed in the adjoint",
+                   "resident_solves": resident, "waves": -(-(nsamples * p.ns) // resident),
+                   "sigma": sigma, "prior": "uniform [1400, 5000] m/s",
+                   "l2": "inputs larger than L2 (wavefield state of the resident solves >> 129 MB)"},
+        "sample_gradients_per_s": sgrad, "plain": plain, "batched_vs_plain": sgrad / plain["sample_gradients_per_s"],
+        "checkpoint_overhead": overhead, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "clocks": clocks, "gpu_launches": launches,
+    }), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -630,6 +785,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "cfg3":
+        run_autograd(args)
     elif args.config == "cfg4":
         run_uneven(args)
     elif args.config == "cfg5":

@@ -49,7 +49,7 @@ class ForwardModel(Function):
 class Posterior:
     def __init__(self, data, config, vel_fixed=1950, sigma=0.1, num_processes=1,
                  log_prior=None, mask=None, paramfile="input_params.txt", device=None,
-                 max_resident=None, hbm_budget=None, graph=True, gradient="reference"):
+                 max_resident=None, hbm_budget=None, graph=True, gradient="reference", checkpoint=False):
         """
         data: observed data with shape (ns*nt*nr,), float32
         config: configparser with the ``[FWI]`` section of the example's config.ini
@@ -64,6 +64,9 @@ class Posterior:
             imaging-condition approximation, in its scaling); "exact" -- dJ/dv
             of the misfit, the exact discrete adjoint of the scheme, which a
             finite difference of ``fwi``'s loss converges to
+        checkpoint: keep the forward state every ~sqrt(nt) steps and recompute
+            each segment in the adjoint instead of storing the whole forward
+            field (1.5x the steps; results bit for bit those of full storage)
         """
         if gradient not in ("reference", "exact"):
             raise ValueError(f"gradient must be 'reference' or 'exact', not {gradient!r}")
@@ -85,7 +88,7 @@ class Posterior:
             raise ValueError(f"mask has {self.mask.size} cells, the model has nz*nx = {self.params.ncell}")
         self.device = torch.device(device if device is not None else "cuda")
         self.engine = Fwi2dEngine(self.params, device=self.device, max_resident=max_resident,
-                                  hbm_budget=hbm_budget, graph=graph)
+                                  hbm_budget=hbm_budget, graph=graph, checkpoint=checkpoint)
         obs = np.ascontiguousarray(np.asarray(data, dtype=np.float32).reshape(-1))
         if obs.size != self.params.data_len:
             raise ValueError(f"data has {obs.size} values, expected ns*nt*nr = {self.params.data_len}")
