@@ -55,7 +55,7 @@ EXPORTED_SYMBOLS = (
     "gb_fwi2d_workspace_bytes", "gb_fwi2d_batch", "gb_fwi2d_last_launch_count",
     "gb_fwi2d_release_caches", "gb_fwi2d_version", "gb_fwi2d_profile_step_ms", "gb_fwi2d_status",
     "gb_fwi2d_batch_noalloc", "gb_fwi2d_tuned_variant", "gb_fwi2d_instances_workspace_bytes",
-    "gb_fwi2d_run_instances", "gb_fwi2d_side_stream_count",
+    "gb_fwi2d_run_instances", "gb_fwi2d_side_stream_count", "gb_fwi2d_instances_waves",
 )
 
 
@@ -127,6 +127,8 @@ def load() -> ctypes.CDLL:
         L.gb_fwi2d_run_instances.argtypes = [I, ctypes.c_int, ctypes.c_uint, ctypes.c_int, ctypes.c_void_p,
                                              ctypes.c_size_t, ctypes.c_void_p]
         L.gb_fwi2d_run_instances.restype = ctypes.c_int
+        L.gb_fwi2d_instances_waves.argtypes = [I, ctypes.c_int, ctypes.c_uint, ctypes.c_int, ctypes.c_size_t]
+        L.gb_fwi2d_instances_waves.restype = ctypes.c_int
         L.gb_fwi2d_side_stream_count.argtypes = []
         L.gb_fwi2d_side_stream_count.restype = ctypes.c_int
         L.gb_fwi2d_release_caches.argtypes = []

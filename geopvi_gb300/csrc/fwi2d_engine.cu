@@ -265,7 +265,8 @@ static int derive(const gb_fwi2d_params &p, Derived &d)
 struct Layout {
     size_t status, vdt, ring, psave, gacc, syn, part, total;
     size_t ring2, ckpt;  // checkpointing only: the adjoint's ring and the stored (p0, p1) pairs
-    size_t store, lam, gpad;  // exact gradient only: forward levels, adjoint levels, padded dJ/dv
+    size_t store, lam, nu, gpad;  // exact gradient only: forward levels, adjoint levels and their
+                                  // a beta lambda, padded dJ/dv
     size_t abeta, cells;      // exact gradient only: per-sample (v dt)^2 beta, the geometry's cell table
     size_t spec;              // pseudo-spectral mode: real field + half spectrum per resident solve
     int resident;
@@ -288,7 +289,8 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Exact gradient: the adjoint needs every forward level, kept either for all
 // nt steps (one segment) or, with checkpointing, for one ceil(sqrt(nt))-step
-// segment at a time: store holds the segment's K+1 levels P^{i0-1} .. P^{i0+K-1}.
+// segment at a time: store holds the segment's levels P^{i0-1} .. P^{i0+K},
+// K+2 of them, which the forward steps write in place.
 static Layout plan_layout_exact(const Geom &g, int nsamples, int resident, bool syn_in_work, bool checkpoint)
 {
     Layout L{};
@@ -303,8 +305,9 @@ static Layout plan_layout_exact(const Geom &g, int nsamples, int resident, bool 
     L.ring = off;   off = align256(off + field * 3 * resident);
     L.ckpt = off;
     if (L.ckpt_nseg > 1) off = align256(off + field * 2 * L.ckpt_nseg * resident);
-    L.store = off;  off = align256(off + field * (L.ckpt_k + 1) * resident);
+    L.store = off;  off = align256(off + field * (L.ckpt_k + 2) * resident);
     L.lam = off;    off = align256(off + field * 3 * resident);
+    L.nu = off;     off = align256(off + field * 3 * resident);
     L.gpad = off;   off = align256(off + field * ninst);
     L.abeta = off;  off = align256(off + field * nsamples);
     L.cells = off;  off = align256(off + sizeof(int4) * (size_t)g.ntz * g.ntx);
@@ -805,7 +808,8 @@ struct Call {
     char *work;
     bool profile;
     Maps maps;
-    Maps maps2;  // checkpointing: the adjoint's ring
+    Maps maps2;  // checkpointing: the adjoint's ring; exact gradient: the store
+    Maps maps3;  // exact gradient: nu beside the adjoint levels
     const float *kk = nullptr;  // pseudo-spectral mode: |k|^2 table on the device
     int variant = 0;            // k_step variant (kStepVariants)
     bool single_stream = false; // never fork onto the side stream (no stream or event is created)
@@ -868,11 +872,7 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
                               (char *)ring + (size_t)((k + 1) % 3) * fbytes, ring_pitch, fbytes, nres,
                               cudaMemcpyDeviceToDevice, st);
         }
-        StepArgs sa;
-        sa.k = k;
-        sa.it = k;
-        sa.snap = -1;
-        sa.rik = c.d->rik[k];
+        const StepArgs sa = ring_step(k, k, -1, c.d->rik[k]);
         launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
     }
     close_span(e0, e1, g.nt);
@@ -891,19 +891,11 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
                           (char *)ck + (size_t)(2 * s + 1) * fbytes, ck_pitch, fbytes, nres,
                           cudaMemcpyDeviceToDevice, st);
         for (int k = k0; k < k1; ++k) {  // recompute the segment's forward steps, storing them
-            StepArgs sa;
-            sa.k = k;
-            sa.it = k;
-            sa.snap = (k % g.nti) == 0 ? k / g.nti - snap0 : -1;
-            sa.rik = c.d->rik[k];
+            const StepArgs sa = ring_step(k, k, (k % g.nti) == 0 ? k / g.nti - snap0 : -1, c.d->rik[k]);
             launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
         }
         for (int it = k1 - 1; it >= k0; --it) {  // the segment's adjoint steps
-            StepArgs sa;
-            sa.k = g.nt - 1 - it;
-            sa.it = it;
-            sa.snap = (it % g.nti) == 0 ? it / g.nti - snap0 : -1;
-            sa.rik = 0.0f;
+            const StepArgs sa = ring_step(g.nt - 1 - it, it, (it % g.nti) == 0 ? it / g.nti - snap0 : -1, 0.0f);
             launches += step(true, c.maps2, g, ba, nres, sa, st, c.variant);
         }
     }
@@ -912,20 +904,21 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
 }
 
 template <int H>
-static void launch_adjoint_exact(const Geom &g, const ExactBatch &x, int nres, int k, int lev1, float rik,
+static void launch_adjoint_exact(const Call &c, const ExactBatch &x, int nres, int k, int lev1, float rik,
                                  cudaStream_t st)
 {
-    const dim3 grid((unsigned)((g.fstride + 255) / 256), nres);
-    k_adjoint_exact<H><<<grid, 256, 0, st>>>(g, x, k, lev1, rik);
+    const Geom &g = c.d->g;
+    const dim3 grid((unsigned)(g.tiles_x * g.tiles_z), nres);
+    k_adjoint_tile<H><<<grid, kAdjThreads, AdjShape<H>::kSmem, st>>>(c.maps3.p1, c.maps2.p1, g, x, k, lev1, rik);
 }
 
-static void adjoint_exact(const Geom &g, const ExactBatch &x, int nres, int k, int lev1, float rik, cudaStream_t st)
+static void adjoint_exact(const Call &c, const ExactBatch &x, int nres, int k, int lev1, float rik, cudaStream_t st)
 {
-    switch (g.Lc - 1) {
-    case 3: launch_adjoint_exact<3>(g, x, nres, k, lev1, rik, st); break;
-    case 4: launch_adjoint_exact<4>(g, x, nres, k, lev1, rik, st); break;
-    case 5: launch_adjoint_exact<5>(g, x, nres, k, lev1, rik, st); break;
-    default: launch_adjoint_exact<6>(g, x, nres, k, lev1, rik, st); break;
+    switch (c.d->g.Lc - 1) {
+    case 3: launch_adjoint_exact<3>(c, x, nres, k, lev1, rik, st); break;
+    case 4: launch_adjoint_exact<4>(c, x, nres, k, lev1, rik, st); break;
+    case 5: launch_adjoint_exact<5>(c, x, nres, k, lev1, rik, st); break;
+    default: launch_adjoint_exact<6>(c, x, nres, k, lev1, rik, st); break;
     }
 }
 
@@ -933,8 +926,9 @@ static void adjoint_exact(const Geom &g, const ExactBatch &x, int nres, int k, i
 // into `store` or a (p0, p1) pair per segment), then the segments from the
 // last: restore the pair, recompute the segment's levels into `store`, and
 // run its adjoint steps k = i1 .. i0+1, each of which needs lambda^{k+1},
-// lambda^{k+2} and the levels P^{k-1}, P^{k-2}.  Levels come out of the
-// forward ring with one strided device copy per step.
+// lambda^{k+2} and the levels P^{k-1}, P^{k-2}.  The forward steps write
+// their levels straight into `store` (a ring of K+2 levels that does not
+// wrap), so no level is copied.
 static long long enqueue_exact(const Call &c, cudaStream_t st)
 {
     const Geom &g = c.d->g;
@@ -945,14 +939,15 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     float *ck = (float *)(c.work + L.ckpt);
     float *store = (float *)(c.work + L.store);
     float *lam = (float *)(c.work + L.lam);
+    float *nu = (float *)(c.work + L.nu);
     float *gpad = (float *)(c.work + L.gpad);
     float *syn = c.syn ? c.syn : (float *)(c.work + L.syn);
     double *part = (double *)(c.work + L.part);
     int *status = (int *)(c.work + L.status);
     const long long ninst = (long long)c.nsamples * g.ns;
-    const int K = L.ckpt_k, nseg = L.ckpt_nseg;
+    const int K = L.ckpt_k, nseg = L.ckpt_nseg, levels = K + 2;
     const size_t fbytes = sizeof(float) * g.fstride;
-    const size_t ring_pitch = 3 * fbytes, store_pitch = (size_t)(K + 1) * fbytes, ck_pitch = 2 * (size_t)nseg * fbytes;
+    const size_t ring_pitch = 3 * fbytes, store_pitch = (size_t)levels * fbytes, ck_pitch = 2 * (size_t)nseg * fbytes;
 
     k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt, c.nsamples);
     float *abeta = (float *)(c.work + L.abeta);
@@ -969,9 +964,13 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     b.obs = c.obs;
     b.syn = syn;
     b.ring = ring;
+    b.levels = 3;
     b.coef = c.tab.coef;
     b.blend_fp32 = c.d->blend_fp32 ? 1 : 0;
     b.status = status;
+    Batch bs = b;  // forward steps writing into the store
+    bs.ring = store;
+    bs.levels = levels;
     ExactBatch x;
     x.vdt = vdt;
     x.abeta = abeta;
@@ -979,60 +978,55 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     x.obs = c.obs;
     x.syn = syn;
     x.lam = lam;
+    x.nu = nu;
     x.store = store;
-    x.store_pitch = (long long)(K + 1) * g.fstride;
+    x.store_pitch = (long long)levels * g.fstride;
+    x.store_levels = levels;
     x.gpad = gpad;
     x.coef = c.tab.coef;
+    x.status = status;
 
-    auto fwd = [&](int it, int nres) {
-        StepArgs sa;
-        sa.k = it;
-        sa.it = it;
-        sa.snap = -1;
-        sa.rik = c.d->rik[it];
-        launches += step(false, c.maps, g, b, nres, sa, st, c.variant);
-    };
-    auto level_out = [&](int it, int slot_level, int nres) {  // P^{it+1} -> store level
-        cudaMemcpy2DAsync((char *)store + (size_t)slot_level * fbytes, store_pitch,
-                          (char *)ring + (size_t)((it + 2) % 3) * fbytes, ring_pitch, fbytes, nres,
-                          cudaMemcpyDeviceToDevice, st);
+    // step it with p0 = store level l, p1 = l + 1, p2 = l + 2
+    auto fwd_store = [&](int it, int l, int nres) {
+        StepArgs sa = ring_step(it, it, -1, c.d->rik[it]);
+        sa.l0 = l;
+        sa.l1 = l + 1;
+        sa.l2 = l + 2;
+        launches += step(false, c.maps2, g, bs, nres, sa, st, c.variant);
     };
     const int wave = (c.flags & GB_FWI2D_PLAIN) ? 1 : L.resident;
     for (long long i0 = 0; i0 < ninst; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
-        b.inst0 = x.inst0 = (int)i0;
-        cudaMemset2DAsync(ring, ring_pitch, 0, 2 * fbytes, nres, st);
-        if (nseg == 1) cudaMemset2DAsync(store, store_pitch, 0, 2 * fbytes, nres, st);  // P^-1 = P^0 = 0
-        for (int it = 0; it < g.nt; ++it) {
-            if (nseg > 1 && it % K == 0) {
-                const int s = it / K;  // the step's (p0, p1) = (P^{it-1}, P^it)
-                for (int h = 0; h < 2; ++h)
-                    cudaMemcpy2DAsync((char *)ck + (size_t)(2 * s + h) * fbytes, ck_pitch,
-                                      (char *)ring + (size_t)((it + h) % 3) * fbytes, ring_pitch, fbytes, nres,
-                                      cudaMemcpyDeviceToDevice, st);
+        b.inst0 = bs.inst0 = x.inst0 = (int)i0;
+        if (nseg == 1) {  // every level in the store: P^-1 = P^0 = 0, step it writes level it + 2
+            cudaMemset2DAsync(store, store_pitch, 0, 2 * fbytes, nres, st);
+            for (int it = 0; it < g.nt; ++it) fwd_store(it, it, nres);
+        } else {
+            cudaMemset2DAsync(ring, ring_pitch, 0, 2 * fbytes, nres, st);
+            for (int it = 0; it < g.nt; ++it) {
+                if (it % K == 0) {
+                    const int s = it / K;  // the step's (p0, p1) = (P^{it-1}, P^it)
+                    for (int h = 0; h < 2; ++h)
+                        cudaMemcpy2DAsync((char *)ck + (size_t)(2 * s + h) * fbytes, ck_pitch,
+                                          (char *)ring + (size_t)((it + h) % 3) * fbytes, ring_pitch, fbytes, nres,
+                                          cudaMemcpyDeviceToDevice, st);
+                }
+                launches += step(false, c.maps, g, b, nres, ring_step(it, it, -1, c.d->rik[it]), st, c.variant);
             }
-            fwd(it, nres);
-            if (nseg == 1 && it <= g.nt - 2) level_out(it, it + 2, nres);
         }
+        // lambda^{nt+1} = lambda^{nt+2} = 0, and nu with them (its pad columns stay zero)
         cudaMemsetAsync(lam, 0, 3 * fbytes * (size_t)nres, st);
+        cudaMemsetAsync(nu, 0, 3 * fbytes * (size_t)nres, st);
         for (int s = nseg - 1; s >= 0; --s) {
             const int i0s = s * K, i1s = std::min(i0s + K, g.nt);
             if (nseg > 1) {
-                // the pair (P^{i0s-1}, P^{i0s}) into the ring's p0, p1 and store levels 0, 1
-                for (int h = 0; h < 2; ++h) {
-                    const char *src = (char *)ck + (size_t)(2 * s + h) * fbytes;
-                    cudaMemcpy2DAsync((char *)ring + (size_t)((i0s + h) % 3) * fbytes, ring_pitch, src, ck_pitch,
-                                      fbytes, nres, cudaMemcpyDeviceToDevice, st);
-                    cudaMemcpy2DAsync((char *)store + (size_t)h * fbytes, store_pitch, src, ck_pitch, fbytes, nres,
-                                      cudaMemcpyDeviceToDevice, st);
-                }
-                for (int it = i0s; it <= i1s - 2; ++it) {
-                    fwd(it, nres);
-                    level_out(it, it - i0s + 2, nres);
-                }
+                // the pair (P^{i0s-1}, P^{i0s}) into store levels 0, 1; recompute the segment
+                cudaMemcpy2DAsync(store, store_pitch, (char *)ck + (size_t)(2 * s) * fbytes, ck_pitch, 2 * fbytes,
+                                  nres, cudaMemcpyDeviceToDevice, st);
+                for (int it = i0s; it <= i1s - 2; ++it) fwd_store(it, it - i0s, nres);
             }
             for (int k = i1s; k >= i0s + 1; --k) {
-                adjoint_exact(g, x, nres, k, k - i0s, c.d->rik[k - 1], st);
+                adjoint_exact(c, x, nres, k, k - i0s, c.d->rik[k - 1], st);
                 ++launches;
             }
         }
@@ -1091,6 +1085,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.spec_resident = c.L.resident;
     b.kk = c.kk;
     b.slot0 = 0;
+    b.levels = 3;
     const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
@@ -1133,11 +1128,8 @@ static long long enqueue(const Call &c, cudaStream_t st)
                 cudaStreamWaitEvent(side->s, side->fork, 0);
             }
             for (int k = 0; k < g.nt; ++k) {
-                StepArgs sa;
-                sa.k = k;
-                sa.it = adj ? g.nt - 1 - k : k;
-                sa.snap = (sa.it % g.nti) == 0 ? sa.it / g.nti : -1;
-                sa.rik = adj ? 0.0f : c.d->rik[sa.it];
+                const int it = adj ? g.nt - 1 - k : k;
+                const StepArgs sa = ring_step(k, it, (it % g.nti) == 0 ? it / g.nti : -1, adj ? 0.0f : c.d->rik[it]);
                 launches += step(adj, maps, g, b, nlo, sa, st, variant, k > 0);
                 if (split) launches += step(adj, maps, g, bhi, nres - nlo, sa, side->s, variant, k > 0);
             }
@@ -1163,6 +1155,364 @@ static long long enqueue(const Call &c, cudaStream_t st)
             syn, c.obs, (long long)g.ns * g.nt * g.nr, part);
         k_misfit_final<<<(c.nsamples + 127) / 128, 128, 0, st>>>(part, c.misfit, c.nsamples);
         launches += 2;
+    }
+    return launches;
+}
+
+// ---------------------------------------------------------------------------
+// Fused launches over instances of different geometry (gb_fwi2d_run_instances)
+//
+// The solves of every instance of a chunk (one FD order, full storage) are
+// packed into waves that fill the caller's workspace; the solves of a wave,
+// whatever their instance, advance together: one k_step_multi launch per time
+// step.  Instances are sorted by nt, longest first, so the solves of a wave
+// have similar time axes and the ones still running at step k are a prefix of
+// the wave -- a launch's grid is that prefix's blocks.  This replaces one
+// launch per instance, wave and step, whose fixed cost dominates small grids
+// (the reference's per-sample loop, geopvi/forward/fwi2d/posterior.py:112-149,
+// runs the instances one after another).
+//
+// Each solve computes exactly what it computes in gb_fwi2d_batch -- the same
+// tile code, its own ring, stored field and gradient slot -- so the results
+// are those of the instances run alone, bit for bit.
+// ---------------------------------------------------------------------------
+struct FusedInst {
+    const gb_fwi2d_instance *x;
+    Derived d;
+    DeviceTables tab;
+    long long ninst;                   // its solves: nsamples * ns
+    size_t vdt, gacc, syn, part, rik;  // buffers kept for the whole chunk (byte offsets in work)
+    size_t keep;                       // their bytes
+    size_t solve_bytes;                // ring and stored field of one resident solve
+};
+
+struct FusedPiece {
+    int inst;             // index of its instance in the chunk
+    int inst0, r;         // solves [inst0, inst0 + r) of that instance
+    size_t ring, psave;   // byte offsets in work
+};
+
+struct FusedWave {
+    std::vector<FusedPiece> pieces;
+    size_t first_off = 0, desc_off = 0;  // its prefix array and descriptors in work
+    int maxnt = 0;
+};
+
+static void fused_inst_sizes(FusedInst &f, bool fwd_only)
+{
+    const Geom &g = f.d.g;
+    f.keep = align256(sizeof(float) * g.fstride * f.x->nsamples);
+    if (!fwd_only) f.keep += align256(sizeof(float) * g.pstride * f.ninst);
+    if (!f.x->syn) f.keep += align256(sizeof(float) * (size_t)f.ninst * g.nt * g.nr);
+    f.keep += align256(sizeof(double) * kMisfitBlocks * f.x->nsamples);
+    f.keep += align256(sizeof(float) * g.nt);
+    f.solve_bytes = sizeof(float) * g.fstride * 3 + (fwd_only ? 0 : sizeof(float) * g.pstride * g.nt_save);
+}
+
+static size_t piece_bytes(const FusedInst &f, int r, bool fwd_only)
+{
+    const Geom &g = f.d.g;
+    return align256(sizeof(float) * g.fstride * 3 * r) +
+           (fwd_only ? 0 : align256(sizeof(float) * g.pstride * g.nt_save * r));
+}
+
+// Upper bound of a chunk's header -- the status word, then every wave's
+// prefix array and descriptors -- for a chunk of `solves` solves: a wave and
+// a piece per solve at most.
+static size_t fused_header_bound(long long solves)
+{
+    return 256 + (size_t)solves * (2 * sizeof(InstanceStep) + 1024);
+}
+
+// The smallest workspace that runs the instance fused: its header bound, its
+// kept buffers and one resident solve.
+static size_t fused_min_bytes(const FusedInst &f, bool fwd_only)
+{
+    return fused_header_bound(f.ninst) + f.keep + piece_bytes(f, 1, fwd_only);
+}
+
+// Flags under which gb_fwi2d_run_instances fuses instances (full storage,
+// the reference's gradient, launches enqueued directly).
+static bool fusable(unsigned flags)
+{
+    return !(flags & (GB_FWI2D_PLAIN | GB_FWI2D_CHECKPOINT | GB_FWI2D_EXACT_GRADIENT | GB_FWI2D_GRAPH |
+                      (0xFu << GB_FWI2D_VARIANT_SHIFT)));
+}
+
+static bool fused_instance(const gb_fwi2d_instance &x, unsigned flags, FusedInst &f)
+{
+    f.x = &x;
+    if (derive(x.params, f.d)) return false;
+    f.ninst = (long long)x.nsamples * f.d.g.ns;
+    fused_inst_sizes(f, (flags & GB_FWI2D_FORWARD_ONLY) != 0);
+    return true;
+}
+
+// Pack the chunk's solves into waves of at most `avail` bytes (and at most
+// max_resident solves when that is positive), in the chunk's order.
+// Returns false when some solve does not fit at all.
+static bool plan_waves(const std::vector<FusedInst> &fi, size_t avail, int max_resident, bool fwd_only,
+                       std::vector<FusedWave> &waves)
+{
+    waves.clear();
+    waves.emplace_back();
+    size_t used = 0;
+    long long res = 0;
+    for (int i = 0; i < (int)fi.size(); ++i) {
+        long long s0 = 0;
+        while (s0 < fi[i].ninst) {
+            const long long left = fi[i].ninst - s0;
+            long long r = used < avail ? (long long)((avail - used) / fi[i].solve_bytes) : 0;
+            r = std::min(r, left);
+            if (max_resident > 0) r = std::min(r, (long long)max_resident - res);
+            while (r > 0 && used + piece_bytes(fi[i], (int)r, fwd_only) > avail) --r;
+            if (r <= 0) {
+                if (waves.back().pieces.empty()) return false;
+                waves.emplace_back();
+                used = 0;
+                res = 0;
+                continue;
+            }
+            FusedPiece pc;
+            pc.inst = i;
+            pc.inst0 = (int)s0;
+            pc.r = (int)r;
+            pc.ring = pc.psave = used;  // relative to the wave's region until placed
+            used += piece_bytes(fi[i], (int)r, fwd_only);
+            res += r;
+            waves.back().pieces.push_back(pc);
+            waves.back().maxnt = std::max(waves.back().maxnt, fi[i].d.g.nt);
+            s0 += r;
+        }
+    }
+    return true;
+}
+
+// How gb_fwi2d_run_instances runs a fusable call: chunks (one FD order each,
+// longest nt first; an instance joins a chunk while the header bound, the
+// kept buffers and one solve of the widest instance still fit), each with
+// its waves; pseudo-spectral instances run alone, after the chunks.
+struct FusedPlan {
+    std::vector<std::vector<FusedInst>> chunks;
+    std::vector<std::vector<FusedWave>> waves;
+    std::vector<int> alone;
+};
+
+static int plan_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
+                          size_t work_bytes, FusedPlan &plan)
+{
+    const bool fwd_only = (flags & GB_FWI2D_FORWARD_ONLY) != 0;
+    std::vector<FusedInst> all(n);
+    for (int i = 0; i < n; ++i)
+        if (!fused_instance(inst[i], flags, all[i])) return GB_FWI2D_EINVAL;
+    std::vector<int> order;
+    for (int i = 0; i < n; ++i) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const Geom &ga = all[a].d.g, &gb = all[b].d.g;
+        return ga.Lc != gb.Lc ? ga.Lc < gb.Lc : ga.nt > gb.nt;
+    });
+    std::vector<FusedInst> chunk;
+    size_t kept = 0, widest = 0;
+    long long solves = 0;
+    auto close = [&]() -> int {
+        if (chunk.empty()) return GB_FWI2D_OK;
+        std::vector<FusedWave> waves;
+        const size_t header = fused_header_bound(solves);
+        if (header + kept >= work_bytes ||
+            !plan_waves(chunk, work_bytes - header - kept, max_resident, fwd_only, waves))
+            return GB_FWI2D_ENOMEM;
+        plan.chunks.push_back(chunk);
+        plan.waves.push_back(waves);
+        chunk.clear();
+        kept = widest = 0;
+        solves = 0;
+        return GB_FWI2D_OK;
+    };
+    for (int idx : order) {
+        FusedInst &f = all[idx];
+        if (f.d.g.pstd) {  // the pseudo-spectral step is not fused
+            plan.alone.push_back(idx);
+            continue;
+        }
+        const size_t w = std::max(widest, piece_bytes(f, 1, fwd_only));
+        if (!chunk.empty() && (chunk[0].d.g.Lc != f.d.g.Lc ||
+                               fused_header_bound(solves + f.ninst) + kept + f.keep + w > work_bytes)) {
+            const int st = close();
+            if (st) return st;
+        }
+        chunk.push_back(f);
+        kept += f.keep;
+        widest = std::max(widest, piece_bytes(f, 1, fwd_only));
+        solves += f.ninst;
+    }
+    return close();
+}
+
+template <int H>
+static void launch_multi(bool adj, const InstanceStep *desc, const int *first, int nact, int blocks, int k,
+                         cudaStream_t st, bool overlap)
+{
+    constexpr StepVariant v = kStepVariants[0];
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = MultiShape<H>::kSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlap ? 1 : 0;
+    const cudaError_t e =
+        adj ? cudaLaunchKernelEx(&cfg, k_step_multi<H, true, v.rows, v.min_blocks>, desc, first, nact, k)
+            : cudaLaunchKernelEx(&cfg, k_step_multi<H, false, v.rows, v.min_blocks>, desc, first, nact, k);
+    if (e != cudaSuccess) t_enqueue_error = GB_FWI2D_ECUDA;
+}
+
+// Enqueue one chunk (instances sorted by nt, longest first, one FD order)
+// laid out as: status word, the waves' tables and the Ricker tables (header),
+// the instances' kept buffers, then one wave region reused by every wave.  Returns the
+// number of kernels enqueued, or -1 when a tensor map or copy failed.
+static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWave> &waves, unsigned flags,
+                                 char *work, cudaStream_t st, bool clear_status)
+{
+    const bool imaging = (flags & GB_FWI2D_IMAGING) != 0;
+    const bool fwd_only = (flags & GB_FWI2D_FORWARD_ONLY) != 0;
+    const bool profile = (flags & GB_FWI2D_PROFILE) != 0;
+    const int H = fi[0].d.g.Lc - 1;
+    int *status = (int *)work;
+    // Tables: per wave its prefix array and descriptors, then the Ricker
+    // tables; within the header bound plus the tables' bytes.
+    size_t off = 256;
+    for (auto &w : waves) {
+        w.first_off = off;
+        off = align256(off + sizeof(int) * (w.pieces.size() + 1));
+        w.desc_off = off;
+        off = align256(off + sizeof(InstanceStep) * w.pieces.size());
+    }
+    long long solves = 0;
+    size_t kept_base = 0;
+    for (auto &f : fi) {
+        f.rik = off;
+        off = align256(off + sizeof(float) * f.d.g.nt);
+        solves += f.ninst;
+        kept_base += align256(sizeof(float) * f.d.g.nt);
+    }
+    const size_t tables_end = off;
+    kept_base += fused_header_bound(solves);  // the waves were planned after this much
+    if (tables_end > kept_base) return -1;
+    off = kept_base;
+    for (auto &f : fi) {  // kept buffers
+        const Geom &g = f.d.g;
+        f.vdt = off;  off = align256(off + sizeof(float) * g.fstride * f.x->nsamples);
+        f.gacc = off; if (!fwd_only) off = align256(off + sizeof(float) * g.pstride * f.ninst);
+        f.syn = off;  if (!f.x->syn) off = align256(off + sizeof(float) * (size_t)f.ninst * g.nt * g.nr);
+        f.part = off; off = align256(off + sizeof(double) * kMisfitBlocks * f.x->nsamples);
+    }
+    const size_t wave_base = off;
+    // Host image of the tables, copied in one transfer.
+    std::vector<char> host(tables_end - 256, 0);
+    auto at = [&](size_t o) { return host.data() + (o - 256); };
+    for (auto &f : fi) std::memcpy(at(f.rik), f.d.rik.data(), sizeof(float) * f.d.g.nt);
+    for (auto &w : waves) {
+        int blocks = 0;
+        size_t used = 0;
+        for (size_t j = 0; j < w.pieces.size(); ++j) {
+            FusedPiece &pc = w.pieces[j];
+            const FusedInst &f = fi[pc.inst];
+            const Geom &g = f.d.g;
+            pc.ring = wave_base + used;
+            pc.psave = pc.ring + align256(sizeof(float) * g.fstride * 3 * pc.r);
+            used += piece_bytes(f, pc.r, fwd_only);
+            InstanceStep d;
+            std::memset(&d, 0, sizeof d);
+            Batch &b = d.b;
+            b.vdt = (float *)(work + f.vdt);
+            b.vel = f.x->vel;
+            b.obs = f.x->obs;
+            b.syn = f.x->syn ? f.x->syn : (float *)(work + f.syn);
+            b.ring = (float *)(work + pc.ring);
+            b.psave = (float *)(work + pc.psave);
+            b.gacc = (float *)(work + f.gacc);
+            b.coef = f.tab.coef;
+            b.blend_fp32 = f.d.blend_fp32 ? 1 : 0;
+            b.status = status;
+            b.inst0 = pc.inst0;
+            b.slot0 = 0;
+            b.levels = 3;
+            b.imaging = imaging ? 1 : 0;
+            b.store = fwd_only ? 0 : 1;
+            if (!make_map(d.tm, b.ring, g, 3LL * pc.r, kBoxX, kTileZ + 2 * (g.Lc - 1))) return -1;
+            d.g = g;
+            d.rik = (const float *)(work + f.rik);
+            d.nres = pc.r;
+            d.first_block = blocks;
+            reinterpret_cast<int *>(at(w.first_off))[j] = blocks;
+            std::memcpy(at(w.desc_off) + sizeof(InstanceStep) * j, &d, sizeof d);
+            blocks += pc.r * g.tiles_x * g.tiles_z;
+        }
+        reinterpret_cast<int *>(at(w.first_off))[w.pieces.size()] = blocks;
+    }
+    // From pageable memory: the copy has taken the host image when it returns.
+    if (cudaMemcpyAsync(work + 256, host.data(), host.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return -1;
+    long long launches = 0;
+    if (clear_status) cudaMemsetAsync(status, 0, sizeof(int), st);
+    for (const auto &f : fi) {
+        const Geom &g = f.d.g;
+        k_prepare<<<grid_for((long long)f.x->nsamples * g.fstride, 256), 256, 0, st>>>(g, f.x->vel,
+                                                                                     (float *)(work + f.vdt),
+                                                                                     f.x->nsamples);
+        ++launches;
+        if (!fwd_only) cudaMemsetAsync(work + f.gacc, 0, sizeof(float) * g.pstride * f.ninst, st);
+    }
+    for (const auto &w : waves) {
+        const InstanceStep *d_desc = (const InstanceStep *)(work + w.desc_off);
+        const int *first = reinterpret_cast<const int *>(at(w.first_off));
+        const int *d_first = (const int *)(work + w.first_off);
+        for (int pass = 0; pass < (fwd_only ? 1 : 2); ++pass) {
+            const bool adj = pass == 1;
+            for (const auto &pc : w.pieces) {  // p0 and p1 of step 0 start at zero (wavefield_initialization)
+                const Geom &g = fi[pc.inst].d.g;
+                cudaMemset2DAsync(work + pc.ring, sizeof(float) * 3 * g.fstride, 0, sizeof(float) * 2 * g.fstride,
+                                  pc.r, st);
+            }
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
+                cudaEventRecord(e0, st);
+            int nact = (int)w.pieces.size();
+            for (int k = 0; k < w.maxnt; ++k) {
+                while (nact > 0 && fi[w.pieces[nact - 1].inst].d.g.nt <= k) --nact;  // the solves still running
+                switch (H) {
+                case 3: launch_multi<3>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
+                case 4: launch_multi<4>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
+                case 5: launch_multi<5>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
+                default: launch_multi<6>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
+                }
+                ++launches;
+            }
+            if (e1) {
+                cudaEventRecord(e1, st);
+                t_profile.spans.emplace_back(e0, e1);
+                t_profile.launches += w.maxnt;
+            }
+        }
+    }
+    for (const auto &f : fi) {
+        const Geom &g = f.d.g;
+        if (f.x->grad && !fwd_only) {
+            k_reduce_grad<<<grid_for((long long)f.x->nsamples * g.nz * g.nx, 256), 256, 0, st>>>(
+                g, (float *)(work + f.gacc), f.x->vel, f.x->grad, f.x->nsamples, imaging ? 1 : 0);
+            ++launches;
+        }
+        if (f.x->misfit) {
+            const float *syn = f.x->syn ? f.x->syn : (const float *)(work + f.syn);
+            k_misfit_partial<<<dim3(kMisfitBlocks, f.x->nsamples), 256, 0, st>>>(
+                syn, f.x->obs, (long long)g.ns * g.nt * g.nr, (double *)(work + f.part));
+            k_misfit_final<<<(f.x->nsamples + 127) / 128, 128, 0, st>>>((double *)(work + f.part), f.x->misfit,
+                                                                         f.x->nsamples);
+            launches += 2;
+        }
     }
     return launches;
 }
@@ -1404,6 +1754,13 @@ static int batch_impl(const gb_fwi2d_params *p, int nsamples, const float *vel, 
     if (ckpt && !exact && !d.g.pstd && !(flags & GB_FWI2D_FORWARD_ONLY) &&
         !make_maps(c.maps2, d.g, (float *)(c.work + L.ring2), L.resident))
         return GB_FWI2D_ECUDA;
+    if (exact && !d.g.pstd && !(flags & GB_FWI2D_FORWARD_ONLY)) {  // the store and nu, as the step's tiles
+        const int box_z = kTileZ + 2 * (d.g.Lc - 1);
+        if (!make_map(c.maps2.p1, (float *)(c.work + L.store), d.g, (long long)(L.ckpt_k + 2) * L.resident, kBoxX,
+                      box_z) ||
+            !make_map(c.maps3.p1, (float *)(c.work + L.nu), d.g, 3LL * L.resident, kBoxX, box_z))
+            return GB_FWI2D_ECUDA;
+    }
     st = get_tables(d, c.tab);
     if (st) return st;
     if (d.g.pstd) {
@@ -1458,8 +1815,11 @@ size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, 
     if (!inst || n <= 0) return 0;
     size_t most = 0;
     for (int i = 0; i < n; ++i) {
-        const size_t b = gb_fwi2d_workspace_bytes(&inst[i].params, inst[i].nsamples, max_resident, flags);
+        size_t b = gb_fwi2d_workspace_bytes(&inst[i].params, inst[i].nsamples, max_resident, flags);
         if (b == 0) return 0;
+        FusedInst f;
+        if (fusable(flags) && inst[i].params.laplace_solver != 1 && fused_instance(inst[i], flags, f))
+            b = fused_min_bytes(f, (flags & GB_FWI2D_FORWARD_ONLY) != 0);
         most = std::max(most, b);
     }
     return most;
@@ -1480,24 +1840,72 @@ int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags,
         const int st = gb_fwi2d_validate(&x.params);
         if (st) return st;
         if (exact && x.params.laplace_solver == 1 && !(flags & GB_FWI2D_FORWARD_ONLY)) return GB_FWI2D_ENOTSUP;
-        if (gb_fwi2d_workspace_bytes(&x.params, x.nsamples, max_resident, flags) > work_bytes)
-            return GB_FWI2D_ENOMEM;
+        if (gb_fwi2d_instances_workspace_bytes(&x, 1, max_resident, flags) > work_bytes) return GB_FWI2D_ENOMEM;
     }
     long long launches = 0;
-    for (int i = 0; i < n; ++i) {
-        const gb_fwi2d_instance &x = inst[i];
-        // The status word is cleared by the first instance only, so a bounded
-        // wait that gave up in any instance stays visible to gb_fwi2d_status.
+    bool first_run = true;  // the status word is cleared once per call
+    // One instance through the gb_fwi2d_batch path (waves as its workspace allows).
+    auto alone = [&](const gb_fwi2d_instance &x) -> int {
         const int st = batch_impl(&x.params, x.nsamples, x.vel, x.obs, x.syn, x.grad, x.misfit, flags,
-                                  max_resident, work, work_bytes, stream, i == 0);
+                                  max_resident, work, work_bytes, stream, first_run);
+        first_run = false;
         launches += t_last_launches;
-        if (st) {
-            t_last_launches = launches;
-            return st;
+        return st;
+    };
+    if (!fusable(flags)) {
+        for (int i = 0; i < n; ++i) {
+            const int st = alone(inst[i]);
+            if (st) {
+                t_last_launches = launches;
+                return st;
+            }
         }
+        t_last_launches = launches;
+        return GB_FWI2D_OK;
     }
+    FusedPlan plan;
+    int st = plan_instances(inst, n, flags, max_resident, work_bytes, plan);
+    if (st) return st;  // not reached: every instance was checked to fit alone
+    cudaGetLastError();
+    cudaStream_t s = (cudaStream_t)stream;
+    for (size_t c = 0; c < plan.chunks.size() && !st; ++c) {
+        for (auto &f : plan.chunks[c]) {
+            st = get_tables(f.d, f.tab);
+            if (st) break;
+        }
+        if (st) break;
+        t_enqueue_error = 0;
+        const long long k = run_fused_chunk(plan.chunks[c], plan.waves[c], flags, (char *)work, s, first_run);
+        first_run = false;
+        if (k < 0) {
+            st = GB_FWI2D_ECUDA;
+            break;
+        }
+        launches += k;
+        st = cudaGetLastError() != cudaSuccess ? GB_FWI2D_ECUDA : t_enqueue_error;
+    }
+    for (size_t i = 0; i < plan.alone.size() && !st; ++i) st = alone(inst[plan.alone[i]]);
     t_last_launches = launches;
-    return GB_FWI2D_OK;
+    return st;
+}
+
+int gb_fwi2d_instances_waves(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
+                             size_t work_bytes)
+{
+    if (!inst || n <= 0 || !fusable(flags)) return GB_FWI2D_EINVAL;
+    for (int i = 0; i < n; ++i) {
+        if (inst[i].nsamples <= 0) return GB_FWI2D_EINVAL;
+        const int st = gb_fwi2d_validate(&inst[i].params);
+        if (st) return st;
+        if (gb_fwi2d_instances_workspace_bytes(&inst[i], 1, max_resident, flags) > work_bytes)
+            return GB_FWI2D_ENOMEM;
+    }
+    FusedPlan plan;
+    const int st = plan_instances(inst, n, flags, max_resident, work_bytes, plan);
+    if (st) return st;
+    int waves = 0;
+    for (const auto &w : plan.waves) waves += (int)w.size();
+    return waves;
 }
 
 long long gb_fwi2d_last_launch_count(void) { return t_last_launches; }

@@ -14,7 +14,7 @@
 // gamma_2 = w_2.  With lambda^k = dJ/dP^k for J = 1/2 sum |R P^{t+1} - obs_t|^2,
 //   lambda^k = R^T r_{k-1} + A1^T lambda^{k+1} + A0^T lambda^{k+2},
 //   dJ/dv_c += lambda^{t+1}_c * d p2_c / d v_c  (step t: p1 = P^t, p0 = P^{t-1}).
-// k_adjoint_exact computes lambda^k for every cell as a gather over the
+// k_adjoint_tile computes lambda^k for every cell as a gather over the
 // cells whose update reads it, and accumulates the padded-grid gradient;
 // k_reduce_exact sums it back onto the interior cells that get_velp's
 // padding replicates.  FP32 arithmetic: this path has no reference output to
@@ -32,10 +32,13 @@ struct ExactBatch {
     const float *obs;      // [ns][nt][nr]
     const float *syn;      // [nsamples*ns][nt][nr]
     float *lam;            // [resident][3][fstride] adjoint levels
+    float *nu;             // [resident][3][fstride] a_c beta_c lambda_c beside each level of lam
     const float *store;    // [resident][levels][fstride] forward levels of the segment
     long long store_pitch; // floats between resident slots of `store`
+    int store_levels;      // levels per resident slot of `store`
     float *gpad;           // [nsamples*ns][fstride] padded-grid dJ/dv
     const BlendCoef *coef; // boundary weights
+    int *status;           // device error word (0 = ok)
     int inst0;
 };
 
@@ -128,117 +131,190 @@ __device__ __forceinline__ Taps taps_of(float s)
 }
 
 // Step k of the backward recursion for every cell of every resident solve:
-// lambda^k into lam[k % 3], and dJ/dv_j += lambda^k_j * d p2_j / d v_j of
-// forward step k-1, whose inputs P^{k-1} and P^{k-2} sit in store levels
-// `lev1` and lev1 - 1.  rik_prev = the Ricker value of step k-1.
+// lambda^k into lam[k % 3] (and nu = a beta lambda^k beside it), and
+// dJ/dv_j += lambda^k_j * d p2_j / d v_j of forward step k-1, whose inputs
+// P^{k-1} and P^{k-2} sit in store levels `lev1` and lev1 - 1.  rik_prev =
+// the Ricker value of step k-1.  lambda^k_j gathers over the cells whose
+// update reads j: R^T r_{k-1} at receivers, the stencil's transpose
+// (a_c beta_c lambda_c of the cross around j, plus 2 beta_j lambda^{k+1}_j -
+// beta_j lambda^{k+2}_j on stencil cells, beta_j lambda^{k+1}_j elsewhere:
+// the copied level) and the blends' transposes within 4 cells of a band.
+//
+// One block per (tile of kTileX x kTileZ cells, resident solve); the two
+// stencil gathers read shared memory, staged by TMA: nu of level k+1 (written
+// beside lambda^{k+1} by the previous step, so a tap of A1^T is one shared
+// load instead of two global ones; zero outside the stencil region, in the
+// pad columns and, by the copy's fill, outside the grid) and the forward
+// level P^{k-1} for the Laplacian of d p2 / d v.  Band taps stay global
+// loads.  Tiles entirely in the stencil region and four or more cells away
+// from every band take constants for their cell facts.
+constexpr int kAdjRowsPerThread = 2;
+constexpr int kAdjThreads = kTileX * kTileZ / kAdjRowsPerThread;  // 256
+
 template <int H>
-__global__ void __launch_bounds__(256)
-    k_adjoint_exact(const Geom g, const ExactBatch b, int k, int lev1, float rik_prev)
+struct AdjShape {
+    static constexpr int kTile = TileShape<H>::kP1Floats;  // floats of one staged tile
+    static constexpr int kBytes = 2 * 4 * kTile;            // TMA bytes per block
+    static constexpr int kSmem = kBytes + 16;               // + the mbarrier
+};
+
+template <int H>
+__global__ void __launch_bounds__(kAdjThreads)
+    k_adjoint_tile(const __grid_constant__ CUtensorMap tm_nu, const __grid_constant__ CUtensorMap tm_store,
+                   const Geom g, const ExactBatch b, int k, int lev1, float rik_prev)
 {
+    using AS = AdjShape<H>;
+    extern __shared__ __align__(1024) float smem[];
+    float *s_nu = smem, *s_p1 = smem + AS::kTile;
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(smem + 2 * AS::kTile);
     const int slot = blockIdx.y;
     const int inst = b.inst0 + slot;
     const int sample = inst / g.ns, shot = inst - sample * g.ns;
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= g.fstride) return;
-    const int iz = (int)(e / g.pitch);
-    const int ix = (int)(e - (long long)iz * g.pitch) - g.xoff;
-    if (ix < 0 || ix >= g.ntx) return;
+    const int trow = blockIdx.x / g.tiles_x, tcol = blockIdx.x - trow * g.tiles_x;
+    const int col0 = tcol * kTileX, row0 = trow * kTileZ;
+    const int lane = threadIdx.x & 31, r0 = threadIdx.x >> 5;  // rows r0 and r0 + kTileZ / 2
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, AS::kBytes);
+        tma_load_3d(s_nu, &tm_nu, &bar, col0 - kHaloX, row0 - H, slot * 3 + (k + 1) % 3);
+        tma_load_3d(s_p1, &tm_store, &bar, col0 - kHaloX, row0 - H, slot * b.store_levels + lev1);
+    }
     const long long P = g.pitch;
-    const long long j = e;
-
     const float *vdt = b.vdt + (long long)sample * g.fstride;
     float *l_base = b.lam + (long long)slot * 3 * g.fstride;
     const float *lam1 = l_base + (long long)((k + 1) % 3) * g.fstride;  // lambda^{k+1}
     const float *lam2 = l_base + (long long)((k + 2) % 3) * g.fstride;  // lambda^{k+2}
     float *lam0 = l_base + (long long)(k % 3) * g.fstride;
-    const float rdx2 = 1.0f / (g.dx * g.dx), rdz2 = 1.0f / (g.dz * g.dz);
-
-    float out = 0.0f;
-    // R^T r_{k-1}: the residual of step k-1 at a receiver cell
-    if (iz == g.r_iz) {
-        const int ir = receiver_of(g, ix);
-        if (ir >= 0) {
-            const long long t = (long long)(k - 1) * g.nr + ir;
-            out += b.syn[(long long)inst * g.nt * g.nr + t] - b.obs[(long long)shot * g.nt * g.nr + t];
-        }
-    }
-    const CellInfo cj = cell_unpack(b.cells[(long long)iz * g.ntx + ix]);
-    // A1^T lambda^{k+1}: nu_c = a_c beta_c lambda_c over the stencil cells c reading j
+    float *nu0 = b.nu + ((long long)slot * 3 + k % 3) * g.fstride;
     const float *ab = b.abeta + (long long)sample * g.fstride;
-    auto nu = [&](int cz, int cx) -> float {
-        if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) return 0.0f;
-        const long long c = (long long)cz * P + cx + g.xoff;
-        return ab[c] * lam1[c];
-    };
-    if (cj.sten) {
-        out += 2.0f * cj.beta * lam1[j] + fd_weight<H>(0) * (rdx2 + rdz2) * nu(iz, ix);
-        out -= cj.beta * lam2[j];  // A0^T lambda^{k+2}
-    } else {
-        out += cj.beta * lam1[j];  // the copied level
-    }
-#pragma unroll
-    for (int m = 1; m <= H; ++m)
-        out += fd_weight<H>(m) * (rdx2 * (nu(iz, ix + m) + nu(iz, ix - m)) + rdz2 * (nu(iz + m, ix) + nu(iz - m, ix)));
-    // Blend taps: cell c = j - kk * step_d (kk <= 4) in blend band d reads p1
-    // at kk <= 2 and p0 at kk <= 4 steps inward of itself.
-    const bool near_band = iz < g.pml + 4 || iz >= g.ntz - g.pml - 4 || ix < g.pml + 4 || ix >= g.ntx - g.pml - 4;
-    if (near_band) {
-#pragma unroll
-        for (int d = 0; d < 4; ++d) {
-            const int sz = d == 0 ? 1 : d == 1 ? -1 : 0, sx = d == 2 ? 1 : d == 3 ? -1 : 0;
-#pragma unroll
-            for (int kk = 0; kk <= 4; ++kk) {
-                const int cz = iz - kk * sz, cx = ix - kk * sx;
-                if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) continue;
-                const CellInfo c = cell_unpack(b.cells[(long long)cz * g.ntx + cx]);
-                const float gam = c.dir[0] == d ? c.gam[0] : c.dir[1] == d ? c.gam[1] : 0.0f;
-                if (gam == 0.0f) continue;
-                const long long ci = (long long)cz * P + cx + g.xoff;
-                const Taps t = taps_of(vdt[ci] / g.dx);
-                const float c1 = kk == 0 ? 2.0f * t.t11 : kk == 1 ? 2.0f * t.t12 : kk == 2 ? 2.0f * t.t13 : 0.0f;
-                const float c0 = kk == 0   ? t.t11 * t.t11
-                                 : kk == 1 ? 2.0f * t.t11 * t.t12
-                                 : kk == 2 ? t.t12 * t.t12 + 2.0f * t.t11 * t.t13
-                                 : kk == 3 ? 2.0f * t.t12 * t.t13
-                                           : t.t13 * t.t13;
-                out += gam * (c1 * lam1[ci] - c0 * lam2[ci]);
-            }
-        }
-    }
-    lam0[j] = out;
-    if (out == 0.0f) return;
-
-    // d p2_j / d v_j of step k-1
     const float *st = b.store + (long long)slot * b.store_pitch;
     const float *p1 = st + (long long)lev1 * g.fstride;
     const float *p0 = p1 - g.fstride;
-    const float v = vdt[j] / g.dt;
-    float d = 0.0f;
-    if (cj.sten) {
-        float lx = fd_weight<H>(0) * p1[j], lz = lx;
+    const float rdx2 = 1.0f / (g.dx * g.dx), rdz2 = 1.0f / (g.dz * g.dz);
+    // Block-uniform: every cell of the tile in the stencil region, no blend
+    // tap within reach (4 cells), so sten = 1, nb = 0, beta = 1.
+    const int ix0 = col0 - g.xoff;
+    const bool plain = ix0 >= g.pml + 4 && ix0 + kTileX <= g.ntx - g.pml - 4 && row0 >= g.pml + 4 &&
+                       row0 + kTileZ <= g.ntz - g.pml - 4;
+
+    // Per cell: the first loads, issued while the tiles are in flight.
+    const int ix = ix0 + lane;
+    float l1v[kAdjRowsPerThread], l2v[kAdjRowsPerThread], abv[kAdjRowsPerThread], vdv[kAdjRowsPerThread];
 #pragma unroll
-        for (int m = 1; m <= H; ++m) {
-            lx += fd_weight<H>(m) * (p1[j + m] + p1[j - m]);
-            lz += fd_weight<H>(m) * (p1[j + m * P] + p1[j - m * P]);
-        }
-        d += cj.beta * 2.0f * v * g.dt * g.dt * (lx * rdx2 + lz * rdz2);
+    for (int q = 0; q < kAdjRowsPerThread; ++q) {
+        const int iz = row0 + r0 + q * (kTileZ / kAdjRowsPerThread);
+        const long long j = (long long)iz * P + col0 + lane;
+        const bool live = ix >= 0 && ix < g.ntx && iz < g.ntz;
+        l1v[q] = live ? __ldg(lam1 + j) : 0.0f;
+        l2v[q] = live ? __ldg(lam2 + j) : 0.0f;
+        abv[q] = live ? __ldg(ab + j) : 0.0f;
+        vdv[q] = live ? __ldg(vdt + j) : 0.0f;
     }
-    if (cj.nb) {
-        const float s = vdt[j] / g.dx;
-        const Taps t = taps_of(s);
-        const float u11 = (2.0f * s - 3.0f) * 0.5f, u12 = 2.0f - 2.0f * s, u13 = (2.0f * s - 1.0f) * 0.5f;  // dt/ds
-        for (int bb = 0; bb < cj.nb; ++bb) {
-            const long long sp = cj.dir[bb] == 0 ? P : cj.dir[bb] == 1 ? -P : cj.dir[bb] == 2 ? 1 : -1;
-            const float dE = 2.0f * (u11 * p1[j] + u12 * p1[j + sp] + u13 * p1[j + 2 * sp]) -
-                             2.0f * t.t11 * u11 * p0[j] - 2.0f * (u11 * t.t12 + t.t11 * u12) * p0[j + sp] -
-                             2.0f * (t.t12 * u12 + u11 * t.t13 + t.t11 * u13) * p0[j + 2 * sp] -
-                             2.0f * (u12 * t.t13 + t.t12 * u13) * p0[j + 3 * sp] -
-                             2.0f * t.t13 * u13 * p0[j + 4 * sp];
-            d += cj.gam[bb] * dE * g.dt / g.dx;
-        }
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        mbar_wait_bounded(&bar, 0);  // the copies may still land: wait again (bounded) before retiring
+        return;
     }
-    if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * g.dt * v;
-    b.gpad[(long long)inst * g.fstride + j] += out * d;
+    if (ix < 0 || ix >= g.ntx) return;
+#pragma unroll
+    for (int q = 0; q < kAdjRowsPerThread; ++q) {
+        const int rr = r0 + q * (kTileZ / kAdjRowsPerThread);
+        const int iz = row0 + rr;
+        if (iz >= g.ntz) break;
+        const long long j = (long long)iz * P + col0 + lane;
+        const float *sn = s_nu + (rr + H) * kBoxX + lane + kHaloX;  // nu^{k+1} at j in the tile
+        float out = 0.0f;
+        if (iz == g.r_iz) {  // R^T r_{k-1}
+            const int ir = receiver_of(g, ix);
+            if (ir >= 0) {
+                const long long t = (long long)(k - 1) * g.nr + ir;
+                out += b.syn[(long long)inst * g.nt * g.nr + t] - b.obs[(long long)shot * g.nt * g.nr + t];
+            }
+        }
+        CellInfo cj;
+        if (plain) {
+            cj.sten = true;
+            cj.nb = 0;
+            cj.dir[0] = cj.dir[1] = -1;
+            cj.beta = 1.0f;
+            cj.gam[0] = cj.gam[1] = 0.0f;
+        } else {
+            cj = cell_unpack(__ldg(b.cells + (long long)iz * g.ntx + ix));
+        }
+        if (cj.sten) {
+            out += 2.0f * cj.beta * l1v[q] + fd_weight<H>(0) * (rdx2 + rdz2) * sn[0];
+            out -= cj.beta * l2v[q];
+        } else {
+            out += cj.beta * l1v[q];
+        }
+#pragma unroll
+        for (int m = 1; m <= H; ++m)
+            out += fd_weight<H>(m) * (rdx2 * (sn[m] + sn[-m]) + rdz2 * (sn[m * kBoxX] + sn[-m * kBoxX]));
+        if (!plain) {
+            const bool near_band =
+                iz < g.pml + 4 || iz >= g.ntz - g.pml - 4 || ix < g.pml + 4 || ix >= g.ntx - g.pml - 4;
+            if (near_band) {
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    const int sz = d == 0 ? 1 : d == 1 ? -1 : 0, sx = d == 2 ? 1 : d == 3 ? -1 : 0;
+#pragma unroll
+                    for (int kk = 0; kk <= 4; ++kk) {
+                        const int cz = iz - kk * sz, cx = ix - kk * sx;
+                        if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) continue;
+                        const CellInfo c = cell_unpack(__ldg(b.cells + (long long)cz * g.ntx + cx));
+                        const float gam = c.dir[0] == d ? c.gam[0] : c.dir[1] == d ? c.gam[1] : 0.0f;
+                        if (gam == 0.0f) continue;
+                        const long long ci = (long long)cz * P + cx + g.xoff;
+                        const Taps t = taps_of(__ldg(vdt + ci) / g.dx);
+                        const float c1 = kk == 0 ? 2.0f * t.t11 : kk == 1 ? 2.0f * t.t12 : kk == 2 ? 2.0f * t.t13 : 0.0f;
+                        const float c0 = kk == 0   ? t.t11 * t.t11
+                                         : kk == 1 ? 2.0f * t.t11 * t.t12
+                                         : kk == 2 ? t.t12 * t.t12 + 2.0f * t.t11 * t.t13
+                                         : kk == 3 ? 2.0f * t.t12 * t.t13
+                                                   : t.t13 * t.t13;
+                        out += gam * (c1 * __ldg(lam1 + ci) - c0 * __ldg(lam2 + ci));
+                    }
+                }
+            }
+        }
+        lam0[j] = out;
+        nu0[j] = abv[q] * out;
+        if (out == 0.0f) continue;
+
+        // d p2_j / d v_j of step k-1
+        const float v = vdv[q] / g.dt;
+        float d = 0.0f;
+        if (cj.sten) {
+            const float *sp1 = s_p1 + (rr + H) * kBoxX + lane + kHaloX;
+            float lx = fd_weight<H>(0) * sp1[0], lz = lx;
+#pragma unroll
+            for (int m = 1; m <= H; ++m) {
+                lx += fd_weight<H>(m) * (sp1[m] + sp1[-m]);
+                lz += fd_weight<H>(m) * (sp1[m * kBoxX] + sp1[-m * kBoxX]);
+            }
+            d += cj.beta * 2.0f * v * g.dt * g.dt * (lx * rdx2 + lz * rdz2);
+        }
+        if (cj.nb) {
+            const float s = vdv[q] / g.dx;
+            const Taps t = taps_of(s);
+            const float u11 = (2.0f * s - 3.0f) * 0.5f, u12 = 2.0f - 2.0f * s, u13 = (2.0f * s - 1.0f) * 0.5f;
+            for (int bb = 0; bb < cj.nb; ++bb) {
+                const long long sp = cj.dir[bb] == 0 ? P : cj.dir[bb] == 1 ? -P : cj.dir[bb] == 2 ? 1 : -1;
+                const float dE = 2.0f * (u11 * p1[j] + u12 * p1[j + sp] + u13 * p1[j + 2 * sp]) -
+                                 2.0f * t.t11 * u11 * p0[j] - 2.0f * (u11 * t.t12 + t.t11 * u12) * p0[j + sp] -
+                                 2.0f * (t.t12 * u12 + u11 * t.t13 + t.t11 * u13) * p0[j + 2 * sp] -
+                                 2.0f * (u12 * t.t13 + t.t12 * u13) * p0[j + 3 * sp] -
+                                 2.0f * t.t13 * u13 * p0[j + 4 * sp];
+                d += cj.gam[bb] * dE * g.dt / g.dx;
+            }
+        }
+        if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * g.dt * v;
+        b.gpad[(long long)inst * g.fstride + j] += out * d;
+    }
 }
 
 // grad[s][cell] = sum over shots and over the padded cells that replicate

@@ -84,7 +84,7 @@ struct Batch {
     const float *vel;    // [nsamples][nz*nx]      inner velocity per sample
     const float *obs;    // [ns][nt][nr]
     float *syn;          // [nsamples*ns][nt][nr]
-    float *ring;         // [resident][3][fstride]
+    float *ring;         // [resident][levels][fstride]
     float *psave;        // [resident][nt_save][pstride]
     float *gacc;         // [nsamples*ns][pstride]
     const BlendCoef *coef;  // [pml0] boundary weight w, 1 - w split in floats and as double
@@ -92,6 +92,7 @@ struct Batch {
     int *status;         // device error word (0 = ok)
     int inst0;           // first solve of this wave
     int slot0;           // first resident slot of this launch (the wave's second half)
+    int levels;          // fields per resident slot of `ring`: 3, or the levels of a stored segment
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
     double *spec;        // pseudo-spectral mode: [resident][ntz][ntx] real array, then the
@@ -103,11 +104,26 @@ struct Batch {
 
 // Per-launch step data.
 struct StepArgs {
-    int k;        // step within the pass: ring buffers (k%3, (k+1)%3, (k+2)%3) = (p0, p1, p2)
+    int k;        // step within the pass
+    int l0, l1, l2;  // ring levels of p0, p1, p2: (k%3, (k+1)%3, (k+2)%3) in a 3-level ring
     int it;       // time index
     int snap;     // snapshot index it/nt_interval, or -1 when it % nt_interval != 0
     float rik;    // Ricker value at it (forward)
 };
+
+// StepArgs of step k of a pass over a 3-level ring.
+__host__ __device__ __forceinline__ StepArgs ring_step(int k, int it, int snap, float rik)
+{
+    StepArgs sa;
+    sa.k = k;
+    sa.l0 = k % 3;
+    sa.l1 = (k + 1) % 3;
+    sa.l2 = (k + 2) % 3;
+    sa.it = it;
+    sa.snap = snap;
+    sa.rik = rik;
+    return sa;
+}
 
 enum : int { kStatusOk = 0, kStatusTmaTimeout = 1 };
 
@@ -488,28 +504,26 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~4.6 KB
 // per block.  The warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
-template <int H, bool ADJ, int U, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB)
-    k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
+// One (solve, tile) of a step: the body of k_step and of k_step_multi.  The
+// tile rank visits tile rows and columns from the edges inward, so the tiles
+// with absorbing strips (the longest) of every solve are dispatched first and
+// each launch ends on interior tiles: a short tail before the next step.
+// `smem` is the block's dynamic shared memory, 1024-byte aligned.
+template <int H, bool ADJ, int U>
+__device__ __forceinline__ void step_tile(const CUtensorMap *tm_p1, const Geom &g, const Batch &b,
+                                          const StepArgs &sa, int solve, int rank, float *smem)
 {
     using TS = TileShape<H>;
-    // Dynamic shared memory only (no static __shared__), so the tile starts
-    // at the 1024-byte aligned base.
-    extern __shared__ __align__(1024) float smem[];
     float *s1 = smem;
     uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
 
-    // blockIdx.x = solve, blockIdx.y = tile rank.  Ranks visit tile rows and
-    // columns from the edges inward, so the tiles with absorbing strips (the
-    // longest) of every solve are dispatched first and each launch ends on
-    // interior tiles: a short tail before the next step.
-    const int slot = b.slot0 + blockIdx.x;
-    const int rr = blockIdx.y / g.tiles_x, cr = blockIdx.y - rr * g.tiles_x;
+    const int slot = b.slot0 + solve;
+    const int rr = rank / g.tiles_x, cr = rank - rr * g.tiles_x;
     const int trow = (rr & 1) ? g.tiles_z - 1 - (rr >> 1) : (rr >> 1);
     const int tcol = (cr & 1) ? g.tiles_x - 1 - (cr >> 1) : (cr >> 1);
     const int col0 = tcol * kTileX;
     const int row0 = trow * kTileZ;
-    const int b0 = sa.k % 3, b1 = (sa.k + 1) % 3, b2 = (sa.k + 2) % 3;
+    const int b0 = sa.l0, b1 = sa.l1, b2 = sa.l2;
 
     // Tiles with no column in [Lc, ntx - Lc): the rim, which neither the
     // stencil nor abc_for_p's passes change from its initial zero (the top and
@@ -520,7 +534,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
         grid_launch_dependents();
         const int ix = col0 - g.xoff + (threadIdx.x & 31);
         if (ix >= 0 && ix < g.ntx) {
-            float *p2 = b.ring + ((long long)slot * 3 + b2) * g.fstride + col0 + (threadIdx.x & 31);
+            float *p2 = b.ring + ((long long)slot * b.levels + b2) * g.fstride + col0 + (threadIdx.x & 31);
             const int iz0 = row0 + (threadIdx.x >> 5) * kWarpRows;
 #pragma unroll 4
             for (int j = 0; j < kWarpRows; ++j)
@@ -541,7 +555,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
     grid_launch_dependents();
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&bar, TS::kBytes);
-        tma_load_3d(s1, &tm_p1, &bar, col0 - kHaloX, row0 - H, slot * 3 + b1);
+        tma_load_3d(s1, tm_p1, &bar, col0 - kHaloX, row0 - H, slot * b.levels + b1);
     }
 
     WarpCtx w;
@@ -557,7 +571,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
     w.iz0 = row0 + w.rr0;
     w.s1 = s1;
     const bool live = w.ix >= 0 && w.ix < g.ntx;
-    float *ring = b.ring + (long long)slot * 3 * g.fstride;
+    float *ring = b.ring + (long long)slot * b.levels * g.fstride;
     w.p0 = ring + (long long)b0 * g.fstride;
     w.p2 = ring + (long long)b2 * g.fstride;
     w.vdt = b.vdt + (long long)w.sample * g.fstride;
@@ -596,6 +610,83 @@ __global__ void __launch_bounds__(kThreads, MINB)
         sweep_interior<H, ADJ, U>(g, b, sa, w, p0_next, vd_next);
     else
         sweep_general<H, ADJ>(g, b, sa, w, p0_next, vd_next);
+}
+
+// One time step of every solve in the wave, one block per (resident slot,
+// tile): blockIdx.x = solve, blockIdx.y = tile rank.
+template <int H, bool ADJ, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    k_step(const __grid_constant__ CUtensorMap tm_p1, const Geom g, const Batch b, const StepArgs sa)
+{
+    // Dynamic shared memory only (no static __shared__), so the tile starts
+    // at the 1024-byte aligned base.
+    extern __shared__ __align__(1024) float smem[];
+    step_tile<H, ADJ, U>(&tm_p1, g, b, sa, blockIdx.x, blockIdx.y, smem);
+}
+
+// One piece of a fused launch over instances of different geometry
+// (gb_fwi2d_run_instances): consecutive solves of one instance, with that
+// instance's geometry, buffers (the ring and stored field of these solves,
+// b.inst0 the first one) and Ricker table, the tensor map over their ring,
+// and where their blocks start in the launch.  Kept in device memory, 64-byte
+// aligned for the tensor map.
+struct __align__(64) InstanceStep {
+    CUtensorMap tm;        // the instance's ring, as k_step's tm_p1
+    Geom g;
+    Batch b;
+    const float *rik;      // [nt] Ricker wavelet (device)
+    int nres;              // its solves (resident slots 0..nres-1 of its ring)
+    int first_block;       // its first block in a launch (also in the launch's prefix array)
+};
+
+// Shared memory of k_step_multi: the tile of k_step, then the block's copy of
+// its instance's geometry and buffers (read throughout the sweep).
+template <int H>
+struct MultiShape {
+    static constexpr int kGeomOff = (TileShape<H>::kSmem + 15) / 16 * 16;
+    static constexpr int kBatchOff = kGeomOff + (int)((sizeof(Geom) + 15) / 16 * 16);
+    static constexpr int kSmem = kBatchOff + (int)sizeof(Batch);
+};
+
+// One time step k of the first `nact` pieces of a wave (sorted by nt,
+// longest first, so the pieces still running at step k are a prefix):
+// block -> piece by binary search of first[] (each piece's first block,
+// ascending), then (solve, tile) as in k_step.  Each piece's time index,
+// snapshot index and Ricker value follow from its own nt and nt_interval.
+template <int H, bool ADJ, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    k_step_multi(const InstanceStep *__restrict__ inst, const int *__restrict__ first, int nact, int k)
+{
+    using MS = MultiShape<H>;
+    extern __shared__ __align__(1024) float smem[];
+    Geom &g = *reinterpret_cast<Geom *>(reinterpret_cast<char *>(smem) + MS::kGeomOff);
+    Batch &b = *reinterpret_cast<Batch *>(reinterpret_cast<char *>(smem) + MS::kBatchOff);
+    int lo = 0, hi = nact - 1;  // the last piece whose first block is <= blockIdx.x
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(first + mid) <= (int)blockIdx.x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const InstanceStep &d = inst[lo];
+    // the piece's geometry and buffers into shared memory
+    static_assert(sizeof(Geom) % 4 == 0 && sizeof(Batch) % 4 == 0, "word copies");
+    const int *gs = reinterpret_cast<const int *>(&d.g);
+    const int *bs = reinterpret_cast<const int *>(&d.b);
+    int *gd = reinterpret_cast<int *>(&g), *bd = reinterpret_cast<int *>(&b);
+    for (int w = threadIdx.x; w < (int)(sizeof(Geom) / 4); w += kThreads) gd[w] = gs[w];
+    for (int w = threadIdx.x; w < (int)(sizeof(Batch) / 4); w += kThreads) bd[w] = bs[w];
+    __syncthreads();
+    const int it = ADJ ? g.nt - 1 - k : k;
+    const StepArgs sa = ring_step(k, it, (it % g.nti) == 0 ? it / g.nti : -1, ADJ ? 0.0f : __ldg(d.rik + it));
+    // The tensor map was copied to device memory before the launch: order
+    // that copy before the asynchronous proxy reads it.
+    if (threadIdx.x == 0)
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&d.tm) : "memory");
+    const int local = (int)blockIdx.x - d.first_block;
+    const int rank = local / d.nres;
+    step_tile<H, ADJ, U>(&d.tm, g, b, sa, local - rank * d.nres, rank, smem);
 }
 
 }  // namespace gbfwi

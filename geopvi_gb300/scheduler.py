@@ -4,12 +4,14 @@ GeoPVI evaluates its likelihood one VI iteration at a time, one sample after
 another (geopvi/forward/fwi2d/posterior.py:112-149).  This module serves many
 such evaluations at once: requests from several inversions (each with its own
 grid, acquisition, time axis and observed data) arrive at any time; a
-dispatcher thread admits them as HBM and streams free up, merges queued
-requests of the same inversion into one batch, chooses how each batch holds
-its forward field (full storage in waves, or sqrt(nt) checkpoints) from a
-cost model, and runs admitted batches concurrently on a pool of CUDA streams.
-Observed data stay resident per inversion; each request's workspace lives
-only while it runs.
+dispatcher thread admits them as HBM and streams free up and merges queued
+requests of the same inversion into one batch.  When several inversions are
+queued, their batches go to the engine in one gb_fwi2d_run_instances call,
+whose waves mix solves of different geometry in one launch per time step;
+a lone batch chooses how it holds its forward field (full storage in waves,
+or sqrt(nt) checkpoints) from a cost model.  Admitted calls run
+concurrently on a pool of CUDA streams.  Observed data stay resident per
+inversion; each call's workspace lives only while it runs.
 
 Every kernel is deterministic and a solve never reads another solve's memory,
 so a request's result does not depend on what ran beside it (the tests check
@@ -31,12 +33,24 @@ import torch
 from . import _native
 from .params import Params
 
-# Cost model of one time step of a wave on GB300, fitted to measured steps
-# (bench plain mode and the cfg2 bench, stored steps): t = LAUNCH_OVERHEAD_S +
-# padded cells / CELL_RATE (one cfg2 solve, 0.11 M cells: 22 us, latency-bound;
-# 183 solves, 20.6 M cells: 131 us).
-CELL_RATE = 1.6e11
+# Cost model of one time step of a wave on GB300: t = LAUNCH_OVERHEAD_S +
+# padded cells x (CELL_S + STRIP_CELL_S x f), f the fraction of the padded
+# grid outside the interior (rim and absorbing strips: the step kernel's
+# general rows, which cost ~2.5x an interior row).  Least-squares fit to the
+# step kernel's measured rates on three grids with full storage of every step
+# (f = 0.07: 1000x2000, 8 solves, 218 G cell-updates/s; f = 0.29: 200x400,
+# 200 solves, 166 G; f = 0.91: 16x32, 4000 solves, 85 G), within 7 % of each;
+# the fixed cost is the latency of one small launch (one 200x400 solve per
+# step: ~22 us).
+CELL_S = 3.78e-12
+STRIP_CELL_S = 8.69e-12
 LAUNCH_OVERHEAD_S = 20e-6
+
+
+def step_seconds(p: Params, resident: int) -> float:
+    """Estimated time of one time step of a wave of `resident` solves."""
+    strip = 1.0 - (p.nx * p.nz) / p.ntp
+    return LAUNCH_OVERHEAD_S + resident * p.ntp * (CELL_S + STRIP_CELL_S * strip)
 
 
 @dataclass
@@ -57,7 +71,7 @@ def plan_batch(p: Params, nsamples: int, cap_bytes: int, lib=None) -> Plan | Non
 
     Full storage runs 2*nt steps per wave; checkpointing 3*nt but needs
     ~sqrt(nt)/nt_save of the stored field, so more solves fit per wave.  A
-    step launch costs LAUNCH_OVERHEAD_S + cells / CELL_RATE."""
+    step launch costs step_seconds(p, resident)."""
     lib = lib or _native.load()
     cp = p.c()
     ninst = nsamples * p.ns
@@ -71,8 +85,7 @@ def plan_batch(p: Params, nsamples: int, cap_bytes: int, lib=None) -> Plan | Non
         r = ninst if per <= 0 else int(min(ninst, 1 + (cap_bytes - base) // per))
         waves = math.ceil(ninst / r)
         steps = (3 if ckpt else 2) * p.nt
-        t_launch = LAUNCH_OVERHEAD_S + r * p.ntp / CELL_RATE
-        est = waves * steps * t_launch
+        est = waves * steps * step_seconds(p, r)
         cand = Plan(resident=r, checkpoint=ckpt, nbytes=_ws(lib, cp, nsamples, r, flags), est_seconds=est)
         if best is None or cand.est_seconds < best.est_seconds:
             best = cand
@@ -142,18 +155,28 @@ class _Inversion:
 
 
 @dataclass
-class _Running:
+class _Part:
+    """One inversion's batch within a call: its requests and output tensors."""
     requests: list
-    stream: torch.cuda.Stream
-    event: torch.cuda.Event
-    work_off: int
-    work_ptr: int
     vel: torch.Tensor
     misfit: torch.Tensor
     grad: torch.Tensor
     syn: torch.Tensor | None
+
+
+@dataclass
+class _Running:
+    parts: list
+    stream: torch.cuda.Stream
+    event: torch.cuda.Event
+    work_off: int
+    work_ptr: int
     plan: Plan
-    inversion: _Inversion
+    keep: object = None  # what the enqueued call points at (instance array)
+
+    @property
+    def requests(self) -> list:
+        return [r for p in self.parts for r in p.requests]
 
 
 class FwiServer:
@@ -201,6 +224,17 @@ class FwiServer:
 
     # ---- requests ----
     def submit(self, name: str, vel, want_syn: bool = False) -> Future:
+        r = self._request(name, vel, want_syn)
+        self._queue.put(r)
+        return r.future
+
+    def submit_many(self, items, want_syn: bool = False) -> list:
+        """Submit [(name, vel), ...] at once: the dispatcher sees all of them together."""
+        reqs = [self._request(name, vel, want_syn) for name, vel in items]
+        self._queue.put(reqs)
+        return [r.future for r in reqs]
+
+    def _request(self, name: str, vel, want_syn: bool) -> Request:
         if name not in self._inv:
             raise KeyError(f"unknown inversion {name!r}")
         vel = vel if isinstance(vel, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(vel, dtype=np.float32))
@@ -212,8 +246,7 @@ class FwiServer:
             raise ValueError("NaN occured in sample!")
         r = Request(name, vel.to(torch.float32), want_syn)
         r.t_submit = time.perf_counter()
-        self._queue.put(r)
-        return r.future
+        return r
 
     def start(self) -> "FwiServer":
         if self._arena_mem is None:
@@ -257,9 +290,10 @@ class FwiServer:
                 progressed = self._reap()
                 while True:
                     try:
-                        self._pending.append(self._queue.get_nowait())
+                        item = self._queue.get_nowait()
                     except queue.Empty:
                         break
+                    self._pending.extend(item if isinstance(item, list) else [item])
                 progressed |= self._admit()
             except Exception as e:  # a failure fails the requests it touched, never the loop
                 for r in self._pending:
@@ -283,24 +317,25 @@ class FwiServer:
             self._running.remove(g)
             try:
                 g.stream.synchronize()
-                misfit = g.misfit.cpu()
-                grad = g.grad.cpu()
-                syn = g.syn.cpu() if g.syn is not None else None
                 st = int(self.lib.gb_fwi2d_status(ctypes.c_void_p(g.work_ptr), ctypes.c_void_p(g.stream.cuda_stream)))
                 now = time.perf_counter()
-                i = 0
-                for r in g.requests:
-                    n = r.nsamples
-                    r.t_done = now
-                    if st != _native.OK:
-                        r.future.set_exception(_native.EngineError(st, "device status"))
-                    else:
-                        res = {"misfit": misfit[i:i + n], "grad": grad[i:i + n]}
-                        if r.want_syn and syn is not None:
-                            res["syn"] = syn[i:i + n]
-                        r.future.set_result(res)
-                    self.completed.append(r)
-                    i += n
+                for part in g.parts:
+                    misfit = part.misfit.cpu()
+                    grad = part.grad.cpu()
+                    syn = part.syn.cpu() if part.syn is not None else None
+                    i = 0
+                    for r in part.requests:
+                        n = r.nsamples
+                        r.t_done = now
+                        if st != _native.OK:
+                            r.future.set_exception(_native.EngineError(st, "device status"))
+                        else:
+                            res = {"misfit": misfit[i:i + n], "grad": grad[i:i + n]}
+                            if r.want_syn and syn is not None:
+                                res["syn"] = syn[i:i + n]
+                            r.future.set_result(res)
+                        self.completed.append(r)
+                        i += n
             except Exception as e:  # pragma: no cover - device errors surface here
                 for r in g.requests:
                     if not r.future.done():
@@ -310,19 +345,57 @@ class FwiServer:
                 self._free_streams.append(g.stream)
         return bool(done)
 
+    def _groups(self) -> list:
+        """Queued requests merged per inversion, in queue order: [(name, [requests], samples)]."""
+        groups: dict = {}
+        for r in self._pending:
+            g = groups.setdefault(r.inversion, [r.inversion, [], 0])
+            if g[2] + r.nsamples <= max(self.max_group_samples, g[1][0].nsamples if g[1] else r.nsamples):
+                g[1].append(r)
+                g[2] += r.nsamples
+        return [tuple(g) for g in groups.values()]
+
+    def _fused_call(self, groups: list, cap: int):
+        """The groups (one imaging mode) that one gb_fwi2d_run_instances call
+        runs in `cap` bytes, and its workspace size; None if fewer than two fit."""
+        imaging = self._inv[groups[0][0]].imaging
+        groups = [g for g in groups if self._inv[g[0]].imaging == imaging]
+        while len(groups) > 1:
+            insts = (_native.CInstance * len(groups))(*[
+                _native.CInstance(self._inv[name].params.c(), n, 1, 1, None, 1, None) for name, _, n in groups])
+            flags = _native.FLAG_IMAGING if imaging else 0
+            need = int(self.lib.gb_fwi2d_instances_workspace_bytes(insts, len(groups), 0, flags))
+            if 0 < need <= cap:
+                # room for every solve resident at once, capped by the arena
+                full = sum(_ws(self.lib, self._inv[name].params.c(), n, 0, flags) for name, _, n in groups)
+                return groups, int(min(cap, full + (8 << 20)))
+            groups = groups[:-1]
+        return None
+
     def _admit(self) -> bool:
         admitted = False
         while self._pending and self._free_streams:
-            head = self._pending[0]
-            inv = self._inv[head.inversion]
-            group, n = [], 0
-            for r in list(self._pending):
-                if r.inversion == head.inversion and n + r.nsamples <= max(self.max_group_samples, head.nsamples):
-                    group.append(r)
-                    n += r.nsamples
+            groups = self._groups()
             free = self._arena.largest()
-            # a batch may take all of the free arena when it runs alone, half otherwise
+            # a call may take all of the free arena when it runs alone, half otherwise
             cap = free if not self._running else free // 2
+            fused = self._fused_call(groups, cap) if len(groups) > 1 else None
+            if fused is not None:
+                sel, nbytes = fused
+                for _, reqs, _ in sel:
+                    for r in reqs:
+                        self._pending.remove(r)
+                try:
+                    self._launch_fused(sel, nbytes)
+                except Exception as e:
+                    for _, reqs, _ in sel:
+                        for r in reqs:
+                            if not r.future.done():
+                                r.future.set_exception(e)
+                admitted = True
+                continue
+            name, group, n = groups[0]
+            inv = self._inv[name]
             plan = plan_batch(inv.params, n, cap, self.lib)
             if plan is None:
                 if not self._running:
@@ -342,6 +415,17 @@ class FwiServer:
             admitted = True
         return admitted
 
+    def _part(self, group: list, inv: _Inversion) -> _Part:
+        """Device inputs and outputs of one inversion's batch (on the current stream)."""
+        p = inv.params
+        n = sum(r.nsamples for r in group)
+        want_syn = any(r.want_syn for r in group)
+        vel = torch.cat([r.vel.to(self.device, non_blocking=True) for r in group]).contiguous()
+        misfit = torch.empty(n, dtype=torch.float64, device=self.device)
+        grad = torch.empty(n, p.ncell, dtype=torch.float32, device=self.device)
+        syn = torch.empty(n, p.data_len, dtype=torch.float32, device=self.device) if want_syn else None
+        return _Part(group, vel, misfit, grad, syn)
+
     def _launch(self, group: list, inv: _Inversion, plan: Plan) -> None:
         off = self._arena.alloc(plan.nbytes)
         if off is None:
@@ -349,22 +433,17 @@ class FwiServer:
         work_ptr = self._arena_mem.data_ptr() + off
         stream = self._free_streams.pop()
         p = inv.params
-        n = sum(r.nsamples for r in group)
-        want_syn = any(r.want_syn for r in group)
         now = time.perf_counter()
         for r in group:
             r.t_start = now
         with torch.cuda.stream(stream):
-            vel = torch.cat([r.vel.to(self.device, non_blocking=True) for r in group]).contiguous()
-            misfit = torch.empty(n, dtype=torch.float64, device=self.device)
-            grad = torch.empty(n, p.ncell, dtype=torch.float32, device=self.device)
-            syn = torch.empty(n, p.data_len, dtype=torch.float32, device=self.device) if want_syn else None
+            part = self._part(group, inv)
             flags = (_native.FLAG_IMAGING if inv.imaging else 0) | (_native.FLAG_CHECKPOINT if plan.checkpoint else 0)
             cp = p.c()
-            st = self.lib.gb_fwi2d_batch(ctypes.byref(cp), n, vel.data_ptr(), inv.obs.data_ptr(),
-                                         syn.data_ptr() if syn is not None else None, grad.data_ptr(),
-                                         misfit.data_ptr(), flags, plan.resident, work_ptr, plan.nbytes,
-                                         ctypes.c_void_p(stream.cuda_stream))
+            st = self.lib.gb_fwi2d_batch(ctypes.byref(cp), part.vel.shape[0], part.vel.data_ptr(),
+                                         inv.obs.data_ptr(), part.syn.data_ptr() if part.syn is not None else None,
+                                         part.grad.data_ptr(), part.misfit.data_ptr(), flags, plan.resident,
+                                         work_ptr, plan.nbytes, ctypes.c_void_p(stream.cuda_stream))
             event = torch.cuda.Event()
             event.record(stream)
         if st != _native.OK:
@@ -373,7 +452,44 @@ class FwiServer:
             for r in group:
                 r.future.set_exception(_native.EngineError(st, "gb_fwi2d_batch"))
             return
-        self._running.append(_Running(group, stream, event, off, work_ptr, vel, misfit, grad, syn, plan, inv))
+        self._running.append(_Running([part], stream, event, off, work_ptr, plan))
+
+    def _launch_fused(self, sel: list, nbytes: int) -> None:
+        """One gb_fwi2d_run_instances call over several inversions' batches."""
+        off = self._arena.alloc(nbytes)
+        if off is None:
+            raise _native.EngineError(_native.ENOMEM, "arena")
+        work_ptr = self._arena_mem.data_ptr() + off
+        stream = self._free_streams.pop()
+        now = time.perf_counter()
+        imaging = self._inv[sel[0][0]].imaging
+        parts, insts = [], []
+        with torch.cuda.stream(stream):
+            for name, group, _ in sel:
+                for r in group:
+                    r.t_start = now
+                inv = self._inv[name]
+                part = self._part(group, inv)
+                parts.append(part)
+                insts.append(_native.CInstance(inv.params.c(), part.vel.shape[0], part.vel.data_ptr(),
+                                               inv.obs.data_ptr(),
+                                               part.syn.data_ptr() if part.syn is not None else None,
+                                               part.grad.data_ptr(), part.misfit.data_ptr()))
+            arr = (_native.CInstance * len(insts))(*insts)
+            flags = _native.FLAG_IMAGING if imaging else 0
+            st = self.lib.gb_fwi2d_run_instances(arr, len(insts), flags, 0, work_ptr, nbytes,
+                                                 ctypes.c_void_p(stream.cuda_stream))
+            event = torch.cuda.Event()
+            event.record(stream)
+        plan = Plan(resident=0, checkpoint=False, nbytes=nbytes, est_seconds=0.0)
+        if st != _native.OK:
+            self._free_streams.append(stream)
+            self._arena.release(off, nbytes)
+            for part in parts:
+                for r in part.requests:
+                    r.future.set_exception(_native.EngineError(st, "gb_fwi2d_run_instances"))
+            return
+        self._running.append(_Running(parts, stream, event, off, work_ptr, plan, keep=arr))
 
 
 def latency_summary(requests: list) -> dict:

@@ -129,22 +129,45 @@ typedef struct gb_fwi2d_instance {
     double *misfit;     /* [nsamples], or NULL */
 } gb_fwi2d_instance;
 
-/* Workspace for gb_fwi2d_run_instances: the largest instance's
- * gb_fwi2d_workspace_bytes (the instances reuse one workspace in stream
- * order); 0 if an instance is invalid. */
+/* The smallest workspace for gb_fwi2d_run_instances; 0 if an instance is
+ * invalid.  Fused instances (below) need their per-instance buffers and one
+ * resident solve of the largest; the others reuse one workspace in stream
+ * order and need the largest instance's gb_fwi2d_workspace_bytes.  A larger
+ * workspace lets more solves share a wave. */
 size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, int max_resident,
                                           unsigned flags);
 
 /* An uneven batch -- instances with different parameter sets -- on one
- * stream, each through the gb_fwi2d_batch path, in order, on one shared
- * workspace.  Every instance is checked before anything is enqueued: an
- * invalid one returns its status (GB_FWI2D_EINVAL, GB_FWI2D_ENOMEM for a
- * workspace too small for it) and nothing runs.  The workspace's status word
- * (gb_fwi2d_status) collects the flags of every instance of the call.  The per-instance
- * descriptor form of the batched API; concurrency across streams and memory
- * admission for mixed workloads are geopvi_gb300/scheduler.py's. */
+ * stream and one workspace.  Replaces the per-sample loop of
+ * geopvi/forward/fwi2d/posterior.py:112-149 for callers whose samples belong
+ * to different inversions.
+ *
+ * Fused (flags without GB_FWI2D_PLAIN, CHECKPOINT, EXACT_GRADIENT, GRAPH or a
+ * forced variant; finite-difference instances): the solves of all instances
+ * of one FD order are packed, longest nt first, into waves that fill
+ * work_bytes (at most max_resident solves each when max_resident > 0), and a
+ * wave advances all its solves -- of any grid, acquisition and time axis --
+ * in one kernel launch per time step, with full storage of the forward
+ * field.  Otherwise, and for pseudo-spectral instances, each instance runs
+ * through the gb_fwi2d_batch path in turn.  Results are bit for bit those of
+ * the instances run alone.
+ *
+ * Every instance is checked before anything is enqueued: an invalid one
+ * returns its status (GB_FWI2D_EINVAL; GB_FWI2D_ENOMEM when work_bytes is
+ * below gb_fwi2d_instances_workspace_bytes) and nothing runs.  The
+ * workspace's status word (gb_fwi2d_status) collects the flags of every
+ * instance of the call.  Concurrency across streams and memory admission for
+ * mixed workloads are geopvi_gb300/scheduler.py's. */
 int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
                            void *work, size_t work_bytes, void *stream);
+
+/* Host only: the number of fused waves gb_fwi2d_run_instances would run for
+ * these instances in work_bytes (pseudo-spectral instances, which run alone,
+ * count none); GB_FWI2D_EINVAL for flags that do not fuse or an invalid
+ * instance, GB_FWI2D_ENOMEM below gb_fwi2d_instances_workspace_bytes.  Lets a
+ * caller size the workspace: more bytes, fewer and wider waves. */
+int gb_fwi2d_instances_waves(const gb_fwi2d_instance *inst, int n, unsigned flags, int max_resident,
+                             size_t work_bytes);
 
 /* Allocation-free variant of gb_fwi2d_batch.  No counterpart in the
  * reference (whose solver allocates and frees its own buffers on every call).

@@ -203,3 +203,31 @@ def test_exact_gradient_workspace_and_flags(engine_lib):
     st = engine_lib.gb_fwi2d_batch(ctypes.byref(small), 1, 1, 1, None, None, None,
                                    _native.FLAG_EXACT_GRADIENT | _native.FLAG_IMAGING, 0, 1, 1 << 30, None)
     assert st == _native.EINVAL
+
+
+def test_step_cost_model_sees_strips_and_launch_latency():
+    """Per padded cell, a small grid (mostly absorbing strips) costs more than a
+    large one, and a one-solve step is dominated by the launch's fixed cost."""
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import LAUNCH_OVERHEAD_S, step_seconds
+    small = workloads.make_params(100, 200, 1500, 1e-3, 4, 8.0)
+    large = workloads.make_params(400, 800, 1500, 1e-3, 4, 8.0)
+    per_cell = lambda p: (step_seconds(p, 1000) - LAUNCH_OVERHEAD_S) / (1000 * p.ntp)  # noqa: E731
+    assert per_cell(small) > 1.2 * per_cell(large)
+    assert step_seconds(small, 1) < 2 * LAUNCH_OVERHEAD_S
+
+
+def test_server_merges_queued_requests_per_inversion():
+    """The dispatcher's groups: one per inversion in queue order, requests of
+    one inversion merged up to max_group_samples (built without a GPU)."""
+    import numpy as np
+    import torch
+    from geopvi_gb300.scheduler import FwiServer, Request
+    srv = FwiServer.__new__(FwiServer)
+    srv.max_group_samples = 8
+    srv._pending = [Request(n, torch.zeros(k, 4)) for n, k in
+                    [("a", 3), ("b", 2), ("a", 4), ("a", 2), ("c", 9), ("b", 1)]]
+    groups = srv._groups()
+    assert [(name, [r.nsamples for r in reqs], n) for name, reqs, n in groups] == [
+        ("a", [3, 4], 7), ("b", [2, 1], 3), ("c", [9], 9)]
+    assert np.sum([n for *_, n in groups]) == 19

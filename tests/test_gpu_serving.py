@@ -2,9 +2,9 @@
 
 Each request's result must be the same alone and in the mix: the server runs
 requests of different grids, acquisitions and time axes concurrently on
-several streams, merges queued requests of one inversion into one batch and
-picks full storage or checkpoints by its HBM budget -- none of which may
-change a single bit of any result.
+several streams or fused into one call, merges queued requests of one
+inversion into one batch and picks full storage or checkpoints by its HBM
+budget -- none of which may change a single bit of any result.
 """
 import os
 import time
@@ -38,8 +38,11 @@ def alone(p, vel, obs):
     return r.misfit.cpu().numpy().copy(), r.grad.cpu().numpy().copy(), r.syn.cpu().numpy().copy()
 
 
-@pytest.mark.parametrize("budget", [150 << 30, 6 << 20])
-def test_uneven_batch_matches_each_job_alone(engine_lib, cuda, budget):
+@pytest.mark.parametrize("budget,at_once", [(150 << 30, False), (6 << 20, False), (150 << 30, True),
+                                             (2 << 20, True)])
+def test_uneven_batch_matches_each_job_alone(engine_lib, cuda, budget, at_once):
+    """at_once: every job reaches the dispatcher together, so the inversions
+    share one fused call (in waves, when the budget is small)."""
     from geopvi_gb300.scheduler import FwiServer
     jobs = []
     for k, name in enumerate(NAMES):
@@ -51,7 +54,11 @@ def test_uneven_batch_matches_each_job_alone(engine_lib, cuda, budget):
     with FwiServer(device="cuda:0", hbm_budget=budget, streams=3) as srv:
         for name, p, vel, obs in jobs:
             srv.register(name, p, obs)
-        futs = {name: srv.submit(name, vel, want_syn=True) for name, p, vel, obs in jobs}
+        if at_once:
+            futs = dict(zip([j[0] for j in jobs], srv.submit_many([(name, vel) for name, _, vel, _ in jobs],
+                                                                  want_syn=True)))
+        else:
+            futs = {name: srv.submit(name, vel, want_syn=True) for name, p, vel, obs in jobs}
         res = {name: f.result(timeout=300) for name, f in futs.items()}
     for name, _, _, _ in jobs:
         m, g, s = expect[name]
