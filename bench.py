@@ -641,7 +641,8 @@ def run_uneven(args):
     print(f"cfg4: observed data for {len(jobs)} instances in {time.perf_counter() - t_setup:.1f} s",
           file=sys.stderr, flush=True)
     cells = sum(cell_updates_per_sample(p) for _, p, _, _ in jobs)
-    with FwiServer(device=dev, streams=4) as srv:
+    budget = int((args.hbm_budget_gb or 200) * (1 << 30))
+    with FwiServer(device=dev, streams=4, hbm_budget=budget) as srv:
         for name, p, _, obs in jobs:
             srv.register(name, p, obs)
         torch.cuda.synchronize(dev)
@@ -659,7 +660,8 @@ def run_uneven(args):
         "config": {"workload": "uneven batch: 48 instances, grids {100x200..400x800}, 4-48 shots, "
                                "nt 1500-5000, Ricker 5-12 Hz, 1 model each, submitted at once",
                    "instances": len(jobs), "cell_updates": cells,
-                   "storage": "one fused gb_fwi2d_run_instances call: full storage, waves of mixed instances"},
+                   "storage": "one fused gb_fwi2d_run_instances call: full storage, waves of mixed instances",
+                   "hbm_budget_gb": budget / (1 << 30)},
         "sample_gradients_per_s": len(jobs) / wall,
         "e2e": {"value": cells / wall, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(sum(v.nbytes for _, _, v, _ in jobs)),

@@ -268,6 +268,7 @@ struct Layout {
     size_t store, lam, nu, gpad;  // exact gradient only: forward levels, adjoint levels and their
                                   // a beta lambda, padded dJ/dv
     size_t abeta, cells;      // exact gradient only: per-sample (v dt)^2 beta, the geometry's cell table
+    size_t taps;              // exact gradient only: per-sample blend taps (kTapPlanes fields)
     size_t spec;              // pseudo-spectral mode: real field + half spectrum per resident solve
     int resident;
     int ckpt_k, ckpt_nseg;  // checkpointing only: steps per segment, segments
@@ -311,6 +312,7 @@ static Layout plan_layout_exact(const Geom &g, int nsamples, int resident, bool 
     L.gpad = off;   off = align256(off + field * ninst);
     L.abeta = off;  off = align256(off + field * nsamples);
     L.cells = off;  off = align256(off + sizeof(int4) * (size_t)g.ntz * g.ntx);
+    L.taps = off;   off = align256(off + field * kTapPlanes * nsamples);
     L.psave = L.gacc = off;
     L.syn = off;
     if (syn_in_work) off = align256(off + sizeof(float) * (size_t)ninst * g.nt * g.nr);
@@ -952,8 +954,9 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     k_prepare<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.vel, vdt, c.nsamples);
     float *abeta = (float *)(c.work + L.abeta);
     int4 *cells = (int4 *)(c.work + L.cells);
+    float *taps = (float *)(c.work + L.taps);
     k_exact_tables<<<grid_for((long long)c.nsamples * g.fstride, 256), 256, 0, st>>>(g, c.tab.coef, vdt, c.nsamples,
-                                                                                   cells, abeta);
+                                                                                   cells, abeta, taps);
     launches += 2;
     if (c.clear_status) cudaMemsetAsync(status, 0, sizeof(int), st);
     cudaMemsetAsync(gpad, 0, fbytes * ninst, st);
@@ -965,6 +968,7 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     b.syn = syn;
     b.ring = ring;
     b.levels = 3;
+    b.tm_slot0 = 0;
     b.coef = c.tab.coef;
     b.blend_fp32 = c.d->blend_fp32 ? 1 : 0;
     b.status = status;
@@ -985,6 +989,10 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     x.gpad = gpad;
     x.coef = c.tab.coef;
     x.status = status;
+    x.taps = taps;
+    x.rdx2 = 1.0f / (g.dx * g.dx);
+    x.rdz2 = 1.0f / (g.dz * g.dz);
+    x.dtdx = g.dt / g.dx;
 
     // step it with p0 = store level l, p1 = l + 1, p2 = l + 2
     auto fwd_store = [&](int it, int l, int nres) {
@@ -1086,6 +1094,7 @@ static long long enqueue(const Call &c, cudaStream_t st)
     b.kk = c.kk;
     b.slot0 = 0;
     b.levels = 3;
+    b.tm_slot0 = 0;
     const Maps &maps = c.maps;
 
     const int wave = plain ? 1 : c.L.resident;
@@ -1192,11 +1201,75 @@ struct FusedPiece {
     size_t ring, psave;   // byte offsets in work
 };
 
+// The pieces of a wave that share a grid (grid_key), at most kMaxPieces:
+// one k_step_multi launch per step.
+struct FusedLaunch {
+    std::vector<int> pieces;  // indices into the wave's pieces, longest nt first
+    int maxnt = 0;
+    MultiArgs args;           // the launch's parameter (the first half of its solves when split)
+    bool split = false;       // the second half runs as its own launch on the side stream
+    MultiArgs args_hi;
+};
+
+// Split a launch's table at solve `at` (among its tm_slot0 order): solves
+// below stay, the rest move to `hi` -- a piece that straddles `at` is cut in
+// two.  Each half's first blocks start again at 0.
+static void split_args(MultiArgs &lo, MultiArgs &hi, int at, const Geom &g, bool fwd_only)
+{
+    MultiArgs all = lo;
+    hi = all;
+    lo.npieces = hi.npieces = 0;
+    int blo = 0, bhi = 0;
+    const int tiles = g.tiles_x * g.tiles_z;
+    for (int q = 0; q < all.npieces; ++q) {
+        const PieceArgs &pc = all.piece[q];
+        const int s0 = pc.tm_slot0, s1 = pc.tm_slot0 + pc.nres;
+        if (s0 < at) {
+            PieceArgs a = pc;
+            a.nres = std::min(s1, at) - s0;
+            a.first_block = blo;
+            lo.first[lo.npieces] = blo;
+            lo.piece[lo.npieces++] = a;
+            blo += a.nres * tiles;
+        }
+        if (s1 > at) {
+            PieceArgs b = pc;
+            const int cut = std::max(0, at - s0);  // solves of this piece in the first half
+            b.inst0 += cut;
+            b.tm_slot0 += cut;
+            b.nres -= cut;
+            b.ring += (size_t)3 * g.fstride * cut;
+            if (!fwd_only) b.psave += (size_t)pc.nt_save * g.pstride * cut;
+            b.first_block = bhi;
+            hi.first[hi.npieces] = bhi;
+            hi.piece[hi.npieces++] = b;
+            bhi += b.nres * tiles;
+        }
+    }
+    lo.first[lo.npieces] = blo;
+    hi.first[hi.npieces] = bhi;
+}
+
 struct FusedWave {
     std::vector<FusedPiece> pieces;
-    size_t first_off = 0, desc_off = 0;  // its prefix array and descriptors in work
+    std::vector<FusedLaunch> launches;
     int maxnt = 0;
 };
+
+// Every Geom field but the acquisition and the time axis, which the pieces
+// of one k_step_multi launch share (the kernel reads them from its parameter).
+static std::vector<long long> grid_key(const Geom &g)
+{
+    std::vector<long long> k = {g.ntx, g.ntz, g.pitch, g.xoff, g.nx, g.nz, g.ipitch, g.ioff, g.pml, g.Lc, g.pml0,
+                                g.tiles_x, g.tiles_z, g.fast_dx, g.fast_dz, g.pstd, g.fstride, g.pstride};
+    uint32_t u;
+    for (float f : {g.dx, g.dz, g.dt, g.rdx, g.rdz, g.fd[0], g.fd[1], g.fd[2], g.fd[3], g.fd[4], g.fd[5], g.fd[6],
+                    g.fd[7]}) {
+        std::memcpy(&u, &f, 4);
+        k.push_back(u);
+    }
+    return k;
+}
 
 static void fused_inst_sizes(FusedInst &f, bool fwd_only)
 {
@@ -1216,27 +1289,21 @@ static size_t piece_bytes(const FusedInst &f, int r, bool fwd_only)
            (fwd_only ? 0 : align256(sizeof(float) * g.pstride * g.nt_save * r));
 }
 
-// Upper bound of a chunk's header -- the status word, then every wave's
-// prefix array and descriptors -- for a chunk of `solves` solves: a wave and
-// a piece per solve at most.
-static size_t fused_header_bound(long long solves)
-{
-    return 256 + (size_t)solves * (2 * sizeof(InstanceStep) + 1024);
-}
+constexpr size_t kFusedHeader = 256;  // the call's status word
 
-// The smallest workspace that runs the instance fused: its header bound, its
+// The smallest workspace that runs the instance fused: the status word, its
 // kept buffers and one resident solve.
 static size_t fused_min_bytes(const FusedInst &f, bool fwd_only)
 {
-    return fused_header_bound(f.ninst) + f.keep + piece_bytes(f, 1, fwd_only);
+    return kFusedHeader + f.keep + piece_bytes(f, 1, fwd_only);
 }
 
 // Flags under which gb_fwi2d_run_instances fuses instances (full storage,
-// the reference's gradient, launches enqueued directly).
+// the reference's gradient, launches enqueued directly; the fused kernel has
+// one variant, so a forced variant does not apply to it).
 static bool fusable(unsigned flags)
 {
-    return !(flags & (GB_FWI2D_PLAIN | GB_FWI2D_CHECKPOINT | GB_FWI2D_EXACT_GRADIENT | GB_FWI2D_GRAPH |
-                      (0xFu << GB_FWI2D_VARIANT_SHIFT)));
+    return !(flags & (GB_FWI2D_PLAIN | GB_FWI2D_CHECKPOINT | GB_FWI2D_EXACT_GRADIENT | GB_FWI2D_GRAPH));
 }
 
 static bool fused_instance(const gb_fwi2d_instance &x, unsigned flags, FusedInst &f)
@@ -1277,7 +1344,7 @@ static bool plan_waves(const std::vector<FusedInst> &fi, size_t avail, int max_r
             pc.inst = i;
             pc.inst0 = (int)s0;
             pc.r = (int)r;
-            pc.ring = pc.psave = used;  // relative to the wave's region until placed
+            pc.ring = pc.psave = 0;  // placed when the chunk runs
             used += piece_bytes(fi[i], (int)r, fwd_only);
             res += r;
             waves.back().pieces.push_back(pc);
@@ -1288,10 +1355,11 @@ static bool plan_waves(const std::vector<FusedInst> &fi, size_t avail, int max_r
     return true;
 }
 
-// How gb_fwi2d_run_instances runs a fusable call: chunks (one FD order each,
-// longest nt first; an instance joins a chunk while the header bound, the
-// kept buffers and one solve of the widest instance still fit), each with
-// its waves; pseudo-spectral instances run alone, after the chunks.
+// How gb_fwi2d_run_instances runs a fusable call: chunks (one FD order each;
+// instances of one grid together, longest nt first; an instance joins a chunk
+// while the status word, the kept buffers and one solve of the widest
+// instance still fit), each with its waves; pseudo-spectral instances run
+// alone, after the chunks.
 struct FusedPlan {
     std::vector<std::vector<FusedInst>> chunks;
     std::vector<std::vector<FusedWave>> waves;
@@ -1307,25 +1375,26 @@ static int plan_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, 
         if (!fused_instance(inst[i], flags, all[i])) return GB_FWI2D_EINVAL;
     std::vector<int> order;
     for (int i = 0; i < n; ++i) order.push_back(i);
+    std::vector<std::vector<long long>> keys(n);
+    for (int i = 0; i < n; ++i) keys[i] = grid_key(all[i].d.g);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         const Geom &ga = all[a].d.g, &gb = all[b].d.g;
-        return ga.Lc != gb.Lc ? ga.Lc < gb.Lc : ga.nt > gb.nt;
+        if (ga.Lc != gb.Lc) return ga.Lc < gb.Lc;
+        if (keys[a] != keys[b]) return keys[a] < keys[b];
+        return ga.nt > gb.nt;
     });
     std::vector<FusedInst> chunk;
     size_t kept = 0, widest = 0;
-    long long solves = 0;
     auto close = [&]() -> int {
         if (chunk.empty()) return GB_FWI2D_OK;
         std::vector<FusedWave> waves;
-        const size_t header = fused_header_bound(solves);
-        if (header + kept >= work_bytes ||
-            !plan_waves(chunk, work_bytes - header - kept, max_resident, fwd_only, waves))
+        if (kFusedHeader + kept >= work_bytes ||
+            !plan_waves(chunk, work_bytes - kFusedHeader - kept, max_resident, fwd_only, waves))
             return GB_FWI2D_ENOMEM;
         plan.chunks.push_back(chunk);
         plan.waves.push_back(waves);
         chunk.clear();
         kept = widest = 0;
-        solves = 0;
         return GB_FWI2D_OK;
     };
     for (int idx : order) {
@@ -1335,28 +1404,36 @@ static int plan_instances(const gb_fwi2d_instance *inst, int n, unsigned flags, 
             continue;
         }
         const size_t w = std::max(widest, piece_bytes(f, 1, fwd_only));
-        if (!chunk.empty() && (chunk[0].d.g.Lc != f.d.g.Lc ||
-                               fused_header_bound(solves + f.ninst) + kept + f.keep + w > work_bytes)) {
+        if (!chunk.empty() && (chunk[0].d.g.Lc != f.d.g.Lc || kFusedHeader + kept + f.keep + w > work_bytes)) {
             const int st = close();
             if (st) return st;
         }
         chunk.push_back(f);
         kept += f.keep;
         widest = std::max(widest, piece_bytes(f, 1, fwd_only));
-        solves += f.ninst;
     }
     return close();
 }
 
-template <int H>
-static void launch_multi(bool adj, const InstanceStep *desc, const int *first, int nact, int blocks, int k,
-                         cudaStream_t st, bool overlap)
+template <int H, int NP>
+static void launch_multi_np(bool adj, const MultiArgs &full, int nact, int k, cudaStream_t st, bool overlap)
 {
     constexpr StepVariant v = kStepVariants[0];
+    MultiArgsN<NP> a;
+    a.tm = full.tm;
+    a.gc = full.gc;
+    a.coef = full.coef;
+    a.status = full.status;
+    a.blend_fp32 = full.blend_fp32;
+    a.imaging = full.imaging;
+    a.store = full.store;
+    a.npieces = full.npieces;
+    for (int q = 0; q <= NP; ++q) a.first[q] = full.first[q];
+    for (int q = 0; q < NP; ++q) a.piece[q] = full.piece[q];
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.gridDim = dim3((unsigned)full.first[nact]);
     cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = MultiShape<H>::kSmem;
+    cfg.dynamicSmemBytes = TileShape<H>::kSmem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1364,15 +1441,29 @@ static void launch_multi(bool adj, const InstanceStep *desc, const int *first, i
     cfg.attrs = attr;
     cfg.numAttrs = overlap ? 1 : 0;
     const cudaError_t e =
-        adj ? cudaLaunchKernelEx(&cfg, k_step_multi<H, true, v.rows, v.min_blocks>, desc, first, nact, k)
-            : cudaLaunchKernelEx(&cfg, k_step_multi<H, false, v.rows, v.min_blocks>, desc, first, nact, k);
+        adj ? cudaLaunchKernelEx(&cfg, k_step_multi<H, true, v.rows, v.min_blocks, NP>, a, nact, k)
+            : cudaLaunchKernelEx(&cfg, k_step_multi<H, false, v.rows, v.min_blocks, NP>, a, nact, k);
     if (e != cudaSuccess) t_enqueue_error = GB_FWI2D_ECUDA;
 }
 
-// Enqueue one chunk (instances sorted by nt, longest first, one FD order)
-// laid out as: status word, the waves' tables and the Ricker tables (header),
-// the instances' kept buffers, then one wave region reused by every wave.  Returns the
-// number of kernels enqueued, or -1 when a tensor map or copy failed.
+// The smallest parameter table that holds the launch's pieces.
+template <int H>
+static void launch_multi(bool adj, const MultiArgs &args, int nact, int k, cudaStream_t st, bool overlap)
+{
+    static_assert(kMaxPieces == 16, "tables of 1, 4 and 16 pieces");
+    if (args.npieces <= 1)
+        launch_multi_np<H, 1>(adj, args, nact, k, st, overlap);
+    else if (args.npieces <= 4)
+        launch_multi_np<H, 4>(adj, args, nact, k, st, overlap);
+    else
+        launch_multi_np<H, 16>(adj, args, nact, k, st, overlap);
+}
+
+// Enqueue one chunk (instances of one FD order, grouped by grid, longest nt
+// first) laid out as: the status word, the instances' kept buffers (Ricker
+// tables first: they are copied from the host in one transfer), then one wave
+// region reused by every wave.  Returns the number of kernels enqueued, or -1
+// when a tensor map or copy failed.
 static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWave> &waves, unsigned flags,
                                  char *work, cudaStream_t st, bool clear_status)
 {
@@ -1381,28 +1472,16 @@ static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWa
     const bool profile = (flags & GB_FWI2D_PROFILE) != 0;
     const int H = fi[0].d.g.Lc - 1;
     int *status = (int *)work;
-    // Tables: per wave its prefix array and descriptors, then the Ricker
-    // tables; within the header bound plus the tables' bytes.
-    size_t off = 256;
-    for (auto &w : waves) {
-        w.first_off = off;
-        off = align256(off + sizeof(int) * (w.pieces.size() + 1));
-        w.desc_off = off;
-        off = align256(off + sizeof(InstanceStep) * w.pieces.size());
-    }
-    long long solves = 0;
-    size_t kept_base = 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    const SideStream *side = side_stream(cs == cudaStreamCaptureStatusNone);
+    size_t off = kFusedHeader;
     for (auto &f : fi) {
         f.rik = off;
         off = align256(off + sizeof(float) * f.d.g.nt);
-        solves += f.ninst;
-        kept_base += align256(sizeof(float) * f.d.g.nt);
     }
     const size_t tables_end = off;
-    kept_base += fused_header_bound(solves);  // the waves were planned after this much
-    if (tables_end > kept_base) return -1;
-    off = kept_base;
-    for (auto &f : fi) {  // kept buffers
+    for (auto &f : fi) {  // the other kept buffers
         const Geom &g = f.d.g;
         f.vdt = off;  off = align256(off + sizeof(float) * g.fstride * f.x->nsamples);
         f.gacc = off; if (!fwd_only) off = align256(off + sizeof(float) * g.pstride * f.ninst);
@@ -1410,51 +1489,94 @@ static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWa
         f.part = off; off = align256(off + sizeof(double) * kMisfitBlocks * f.x->nsamples);
     }
     const size_t wave_base = off;
-    // Host image of the tables, copied in one transfer.
-    std::vector<char> host(tables_end - 256, 0);
-    auto at = [&](size_t o) { return host.data() + (o - 256); };
-    for (auto &f : fi) std::memcpy(at(f.rik), f.d.rik.data(), sizeof(float) * f.d.g.nt);
+    std::vector<char> host(tables_end - kFusedHeader, 0);
+    for (auto &f : fi) std::memcpy(host.data() + (f.rik - kFusedHeader), f.d.rik.data(), sizeof(float) * f.d.g.nt);
+
     for (auto &w : waves) {
-        int blocks = 0;
-        size_t used = 0;
-        for (size_t j = 0; j < w.pieces.size(); ++j) {
-            FusedPiece &pc = w.pieces[j];
-            const FusedInst &f = fi[pc.inst];
-            const Geom &g = f.d.g;
-            pc.ring = wave_base + used;
-            pc.psave = pc.ring + align256(sizeof(float) * g.fstride * 3 * pc.r);
-            used += piece_bytes(f, pc.r, fwd_only);
-            InstanceStep d;
-            std::memset(&d, 0, sizeof d);
-            Batch &b = d.b;
-            b.vdt = (float *)(work + f.vdt);
-            b.vel = f.x->vel;
-            b.obs = f.x->obs;
-            b.syn = f.x->syn ? f.x->syn : (float *)(work + f.syn);
-            b.ring = (float *)(work + pc.ring);
-            b.psave = (float *)(work + pc.psave);
-            b.gacc = (float *)(work + f.gacc);
-            b.coef = f.tab.coef;
-            b.blend_fp32 = f.d.blend_fp32 ? 1 : 0;
-            b.status = status;
-            b.inst0 = pc.inst0;
-            b.slot0 = 0;
-            b.levels = 3;
-            b.imaging = imaging ? 1 : 0;
-            b.store = fwd_only ? 0 : 1;
-            if (!make_map(d.tm, b.ring, g, 3LL * pc.r, kBoxX, kTileZ + 2 * (g.Lc - 1))) return -1;
-            d.g = g;
-            d.rik = (const float *)(work + f.rik);
-            d.nres = pc.r;
-            d.first_block = blocks;
-            reinterpret_cast<int *>(at(w.first_off))[j] = blocks;
-            std::memcpy(at(w.desc_off) + sizeof(InstanceStep) * j, &d, sizeof d);
-            blocks += pc.r * g.tiles_x * g.tiles_z;
+        // Launches: the wave's pieces by grid, in order of first appearance,
+        // at most kMaxPieces - 1 each (a split cuts one piece in two).
+        w.launches.clear();
+        std::vector<std::vector<long long>> keys;
+        for (int j = 0; j < (int)w.pieces.size(); ++j) {
+            const auto key = grid_key(fi[w.pieces[j].inst].d.g);
+            size_t c = 0;
+            while (c < keys.size() && !(keys[c] == key && (int)w.launches[c].pieces.size() < kMaxPieces - 1)) ++c;
+            if (c == keys.size()) {
+                keys.push_back(key);
+                w.launches.emplace_back();
+            }
+            w.launches[c].pieces.push_back(j);
+            w.launches[c].maxnt = std::max(w.launches[c].maxnt, fi[w.pieces[j].inst].d.g.nt);
         }
-        reinterpret_cast<int *>(at(w.first_off))[w.pieces.size()] = blocks;
+        // Per launch: its pieces' rings back to back (one tensor map covers
+        // them), then their stored fields; within the planned bytes, which
+        // counted each ring rounded up on its own.
+        size_t used = 0;
+        for (auto &l : w.launches) {
+            const FusedInst &f0 = fi[w.pieces[l.pieces[0]].inst];
+            const Geom &g0 = f0.d.g;
+            MultiArgs &A = l.args;
+            std::memset(&A, 0, sizeof A);
+            const size_t base = wave_base + used;
+            int slots = 0, blocks = 0;
+            for (size_t q = 0; q < l.pieces.size(); ++q) {
+                FusedPiece &pc = w.pieces[l.pieces[q]];
+                const FusedInst &f = fi[pc.inst];
+                const Geom &g = f.d.g;
+                pc.ring = base + sizeof(float) * g.fstride * 3 * slots;
+                PieceArgs &P = A.piece[q];
+                P.vdt = (const float *)(work + f.vdt);
+                P.vel = f.x->vel;
+                P.obs = f.x->obs;
+                P.rik = (const float *)(work + f.rik);
+                P.syn = f.x->syn ? f.x->syn : (float *)(work + f.syn);
+                P.ring = (float *)(work + pc.ring);
+                P.gacc = (float *)(work + f.gacc);
+                P.s_iz = g.s_iz;
+                P.r_iz = g.r_iz;
+                P.r_ix0 = g.r_ix0;
+                P.dr = g.dr;
+                P.nr = g.nr;
+                P.ds = g.ds;
+                P.s_ix0 = g.s_ix0;
+                P.ns = g.ns;
+                P.nt = g.nt;
+                P.nti = g.nti;
+                P.nt_save = g.nt_save;
+                P.inst0 = pc.inst0;
+                P.tm_slot0 = slots;
+                P.nres = pc.r;
+                P.first_block = blocks;
+                A.first[q] = blocks;
+                slots += pc.r;
+                blocks += pc.r * g.tiles_x * g.tiles_z;
+            }
+            A.first[l.pieces.size()] = blocks;
+            used = align256(used + sizeof(float) * g0.fstride * 3 * slots);
+            for (size_t q = 0; q < l.pieces.size(); ++q) {
+                FusedPiece &pc = w.pieces[l.pieces[q]];
+                const Geom &g = fi[pc.inst].d.g;
+                pc.psave = wave_base + used;
+                A.piece[q].psave = (float *)(work + pc.psave);
+                if (!fwd_only) used = align256(used + sizeof(float) * g.pstride * g.nt_save * pc.r);
+            }
+            if (!make_map(A.tm, work + base, g0, 3LL * slots, kBoxX, kTileZ + 2 * (g0.Lc - 1))) return -1;
+            A.gc = g0;
+            A.coef = f0.tab.coef;
+            A.status = status;
+            A.blend_fp32 = f0.d.blend_fp32 ? 1 : 0;
+            A.imaging = imaging ? 1 : 0;
+            A.store = fwd_only ? 0 : 1;
+            A.npieces = (int)l.pieces.size();
+            // Launches of at least kSplitMinResident solves run as two halves on
+            // two streams, so the tail of one half's step overlaps the other's.
+            l.split = side != nullptr && slots >= kSplitMinResident;
+            if (l.split) split_args(A, l.args_hi, slots / 2, g0, fwd_only);
+        }
     }
     // From pageable memory: the copy has taken the host image when it returns.
-    if (cudaMemcpyAsync(work + 256, host.data(), host.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    if (!host.empty() &&
+        cudaMemcpyAsync(work + kFusedHeader, host.data(), host.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
         return -1;
     long long launches = 0;
     if (clear_status) cudaMemsetAsync(status, 0, sizeof(int), st);
@@ -1467,9 +1589,6 @@ static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWa
         if (!fwd_only) cudaMemsetAsync(work + f.gacc, 0, sizeof(float) * g.pstride * f.ninst, st);
     }
     for (const auto &w : waves) {
-        const InstanceStep *d_desc = (const InstanceStep *)(work + w.desc_off);
-        const int *first = reinterpret_cast<const int *>(at(w.first_off));
-        const int *d_first = (const int *)(work + w.first_off);
         for (int pass = 0; pass < (fwd_only ? 1 : 2); ++pass) {
             const bool adj = pass == 1;
             for (const auto &pc : w.pieces) {  // p0 and p1 of step 0 start at zero (wavefield_initialization)
@@ -1480,21 +1599,47 @@ static long long run_fused_chunk(std::vector<FusedInst> &fi, std::vector<FusedWa
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (profile && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
                 cudaEventRecord(e0, st);
-            int nact = (int)w.pieces.size();
-            for (int k = 0; k < w.maxnt; ++k) {
-                while (nact > 0 && fi[w.pieces[nact - 1].inst].d.g.nt <= k) --nact;  // the solves still running
+            bool forked = false;
+            for (const auto &l : w.launches) forked |= l.split;
+            if (forked) {  // fork: the second halves' chain on the side stream
+                cudaEventRecord(side->fork, st);
+                cudaStreamWaitEvent(side->s, side->fork, 0);
+            }
+            std::vector<int> nact, nact_hi;
+            for (const auto &l : w.launches) {
+                nact.push_back(l.args.npieces);
+                nact_hi.push_back(l.split ? l.args_hi.npieces : 0);
+            }
+            // Each step waits for the launch before it on its stream; the first
+            // of a pass on each stream follows the rings' reset and launches normally.
+            bool started = false, started_hi = false;
+            auto launch = [&](const MultiArgs &a, int &na, int k, cudaStream_t s, bool &on) {
+                while (na > 0 && a.piece[na - 1].nt <= k) --na;  // the pieces still running: a prefix
+                if (na == 0) return;
                 switch (H) {
-                case 3: launch_multi<3>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
-                case 4: launch_multi<4>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
-                case 5: launch_multi<5>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
-                default: launch_multi<6>(adj, d_desc, d_first, nact, first[nact], k, st, k > 0); break;
+                case 3: launch_multi<3>(adj, a, na, k, s, on); break;
+                case 4: launch_multi<4>(adj, a, na, k, s, on); break;
+                case 5: launch_multi<5>(adj, a, na, k, s, on); break;
+                default: launch_multi<6>(adj, a, na, k, s, on); break;
                 }
+                on = true;
                 ++launches;
+            };
+            for (int k = 0; k < w.maxnt; ++k) {
+                for (size_t li = 0; li < w.launches.size(); ++li) {
+                    const FusedLaunch &l = w.launches[li];
+                    launch(l.args, nact[li], k, st, started);
+                    if (l.split) launch(l.args_hi, nact_hi[li], k, side->s, started_hi);
+                }
+            }
+            if (forked) {  // join
+                cudaEventRecord(side->join, side->s);
+                cudaStreamWaitEvent(st, side->join, 0);
             }
             if (e1) {
                 cudaEventRecord(e1, st);
                 t_profile.spans.emplace_back(e0, e1);
-                t_profile.launches += w.maxnt;
+                for (const auto &l : w.launches) t_profile.launches += l.maxnt * (l.split ? 2 : 1);
             }
         }
     }

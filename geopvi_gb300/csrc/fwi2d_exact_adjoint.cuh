@@ -37,10 +37,20 @@ struct ExactBatch {
     long long store_pitch; // floats between resident slots of `store`
     int store_levels;      // levels per resident slot of `store`
     float *gpad;           // [nsamples*ns][fstride] padded-grid dJ/dv
+    const float *taps;     // [nsamples][16][fstride] blend taps per cell: kBandZ.. then kBandX..
     const BlendCoef *coef; // boundary weights
     int *status;           // device error word (0 = ok)
+    float rdx2, rdz2;      // 1 / dx^2, 1 / dz^2
+    float dtdx;            // dt / dx: d s / d v for s = v dt / dx
     int inst0;
 };
+
+// Planes of ExactBatch::taps for one sample: for the z blend (top / bottom
+// band) of a cell c and then for its x blend (left / right), its weight
+// gamma times the coefficients of p1 at 0, 1, 2 steps inward (2 t11, 2 t12,
+// 2 t13) and of p0 at 0..4 steps inward (t11^2, 2 t11 t12, t12^2 + 2 t11 t13,
+// 2 t12 t13, t13^2): the entries of A1 and A0 that the blend puts in row c.
+constexpr int kBandZ = 0, kBandX = 8, kTapPlanes = 16;
 
 // Blend facts of one padded cell: blends applied in order (top/bottom, then
 // left/right), their inward steps and weights, beta and gamma.
@@ -97,9 +107,18 @@ __device__ __forceinline__ CellInfo cell_unpack(int4 v)
     return c;
 }
 
-// The geometry's cell table and each sample's (v dt)^2 beta field.
+// Extrapolation weights of s = v dt / dx (abc_for_p's t11, t12, t13).
+struct Taps {
+    float t11, t12, t13;
+};
+__device__ __forceinline__ Taps taps_of(float s)
+{
+    return Taps{(2.0f - s) * (1.0f - s) * 0.5f, s * (2.0f - s), s * (s - 1.0f) * 0.5f};
+}
+
+// The geometry's cell table and each sample's (v dt)^2 beta field and blend taps.
 __global__ void k_exact_tables(const Geom g, const BlendCoef *coef, const float *__restrict__ vdt, int nsamples,
-                               int4 *__restrict__ cells, float *__restrict__ abeta)
+                               int4 *__restrict__ cells, float *__restrict__ abeta, float *__restrict__ taps)
 {
     const long long n = (long long)g.ntz * g.ntx;
     for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
@@ -112,23 +131,25 @@ __global__ void k_exact_tables(const Geom g, const BlendCoef *coef, const float 
          e += (long long)gridDim.x * blockDim.x) {
         const long long r = e % g.fstride;
         const int iz = (int)(r / g.pitch), ix = (int)(r - (long long)iz * g.pitch) - g.xoff;
-        float a = 0.0f;
+        float a = 0.0f, gz = 0.0f, gx = 0.0f;
         if (ix >= 0 && ix < g.ntx) {
             const CellInfo c = cell_info(g, coef, iz, ix);
             if (c.sten) a = vdt[e] * vdt[e] * c.beta;
+            for (int bb = 0; bb < c.nb; ++bb) (c.dir[bb] <= 1 ? gz : gx) = c.gam[bb];
         }
         abeta[e] = a;
+        const Taps t = taps_of(vdt[e] / g.dx);
+        const float cf[8] = {2.0f * t.t11, 2.0f * t.t12, 2.0f * t.t13, t.t11 * t.t11, 2.0f * t.t11 * t.t12,
+                             t.t12 * t.t12 + 2.0f * t.t11 * t.t13, 2.0f * t.t12 * t.t13, t.t13 * t.t13};
+        float *tp = taps + (e / g.fstride) * kTapPlanes * g.fstride + r;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            tp[(kBandZ + q) * g.fstride] = gz * cf[q];
+            tp[(kBandX + q) * g.fstride] = gx * cf[q];
+        }
     }
 }
 
-// Extrapolation weights of s = v dt / dx (abc_for_p's t11, t12, t13).
-struct Taps {
-    float t11, t12, t13;
-};
-__device__ __forceinline__ Taps taps_of(float s)
-{
-    return Taps{(2.0f - s) * (1.0f - s) * 0.5f, s * (2.0f - s), s * (s - 1.0f) * 0.5f};
-}
 
 // Step k of the backward recursion for every cell of every resident solve:
 // lambda^k into lam[k % 3] (and nu = a beta lambda^k beside it), and
@@ -148,8 +169,9 @@ __device__ __forceinline__ Taps taps_of(float s)
 // level P^{k-1} for the Laplacian of d p2 / d v.  Band taps stay global
 // loads.  Tiles entirely in the stencil region and four or more cells away
 // from every band take constants for their cell facts.
-constexpr int kAdjRowsPerThread = 2;
+constexpr int kAdjRowsPerThread = 2;                              // rows r0 and r0 + kTileZ / 2
 constexpr int kAdjThreads = kTileX * kTileZ / kAdjRowsPerThread;  // 256
+constexpr int kAdjMinBlocks = 5;  // resident blocks per SM: each waits on its tiles' copy first
 
 template <int H>
 struct AdjShape {
@@ -159,10 +181,11 @@ struct AdjShape {
 };
 
 template <int H>
-__global__ void __launch_bounds__(kAdjThreads)
+__global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
     k_adjoint_tile(const __grid_constant__ CUtensorMap tm_nu, const __grid_constant__ CUtensorMap tm_store,
                    const Geom g, const ExactBatch b, int k, int lev1, float rik_prev)
 {
+    constexpr int R = kAdjRowsPerThread, RS = kTileZ / R;  // rows per thread, their spacing
     using AS = AdjShape<H>;
     extern __shared__ __align__(1024) float smem[];
     float *s_nu = smem, *s_p1 = smem + AS::kTile;
@@ -172,7 +195,7 @@ __global__ void __launch_bounds__(kAdjThreads)
     const int sample = inst / g.ns, shot = inst - sample * g.ns;
     const int trow = blockIdx.x / g.tiles_x, tcol = blockIdx.x - trow * g.tiles_x;
     const int col0 = tcol * kTileX, row0 = trow * kTileZ;
-    const int lane = threadIdx.x & 31, r0 = threadIdx.x >> 5;  // rows r0 and r0 + kTileZ / 2
+    const int lane = threadIdx.x & 31, rr0 = threadIdx.x >> 5;  // tile rows rr0 + q * RS
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
@@ -194,7 +217,7 @@ __global__ void __launch_bounds__(kAdjThreads)
     const float *st = b.store + (long long)slot * b.store_pitch;
     const float *p1 = st + (long long)lev1 * g.fstride;
     const float *p0 = p1 - g.fstride;
-    const float rdx2 = 1.0f / (g.dx * g.dx), rdz2 = 1.0f / (g.dz * g.dz);
+    const float rdx2 = b.rdx2, rdz2 = b.rdz2;
     // Block-uniform: every cell of the tile in the stencil region, no blend
     // tap within reach (4 cells), so sten = 1, nb = 0, beta = 1.
     const int ix0 = col0 - g.xoff;
@@ -203,30 +226,31 @@ __global__ void __launch_bounds__(kAdjThreads)
 
     // Per cell: the first loads, issued while the tiles are in flight.
     const int ix = ix0 + lane;
-    float l1v[kAdjRowsPerThread], l2v[kAdjRowsPerThread], abv[kAdjRowsPerThread], vdv[kAdjRowsPerThread];
+    const bool col_live = ix >= 0 && ix < g.ntx;
+    const long long j0 = (long long)(row0 + rr0) * P + col0 + lane;
+    float l1v[R], l2v[R], abv[R], vdv[R];
 #pragma unroll
-    for (int q = 0; q < kAdjRowsPerThread; ++q) {
-        const int iz = row0 + r0 + q * (kTileZ / kAdjRowsPerThread);
-        const long long j = (long long)iz * P + col0 + lane;
-        const bool live = ix >= 0 && ix < g.ntx && iz < g.ntz;
-        l1v[q] = live ? __ldg(lam1 + j) : 0.0f;
-        l2v[q] = live ? __ldg(lam2 + j) : 0.0f;
-        abv[q] = live ? __ldg(ab + j) : 0.0f;
-        vdv[q] = live ? __ldg(vdt + j) : 0.0f;
+    for (int q = 0; q < R; ++q) {
+        const bool live = col_live && row0 + rr0 + q * RS < g.ntz;
+        l1v[q] = live ? __ldg(lam1 + j0 + q * RS * P) : 0.0f;
+        l2v[q] = live ? __ldg(lam2 + j0 + q * RS * P) : 0.0f;
+        abv[q] = live ? __ldg(ab + j0 + q * RS * P) : 0.0f;
+        vdv[q] = live ? __ldg(vdt + j0 + q * RS * P) : 0.0f;
     }
     if (!mbar_wait_bounded(&bar, 0)) {
         if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
         mbar_wait_bounded(&bar, 0);  // the copies may still land: wait again (bounded) before retiring
         return;
     }
-    if (ix < 0 || ix >= g.ntx) return;
+    if (!col_live) return;
+    const int sc = lane + kHaloX;
 #pragma unroll
-    for (int q = 0; q < kAdjRowsPerThread; ++q) {
-        const int rr = r0 + q * (kTileZ / kAdjRowsPerThread);
+    for (int q = 0; q < R; ++q) {
+        const int rr = rr0 + q * RS;
         const int iz = row0 + rr;
         if (iz >= g.ntz) break;
-        const long long j = (long long)iz * P + col0 + lane;
-        const float *sn = s_nu + (rr + H) * kBoxX + lane + kHaloX;  // nu^{k+1} at j in the tile
+        const long long j = j0 + q * RS * P;
+        const float *sn = s_nu + (rr + H) * kBoxX + sc;  // nu^{k+1} at j in the tile
         float out = 0.0f;
         if (iz == g.r_iz) {  // R^T r_{k-1}
             const int ir = receiver_of(g, ix);
@@ -255,29 +279,49 @@ __global__ void __launch_bounds__(kAdjThreads)
         for (int m = 1; m <= H; ++m)
             out += fd_weight<H>(m) * (rdx2 * (sn[m] + sn[-m]) + rdz2 * (sn[m * kBoxX] + sn[-m * kBoxX]));
         if (!plain) {
-            const bool near_band =
-                iz < g.pml + 4 || iz >= g.ntz - g.pml - 4 || ix < g.pml + 4 || ix >= g.ntx - g.pml - 4;
-            if (near_band) {
+            // A1^T and A0^T of the blends: cells c whose band's extrapolation
+            // reads j, 0..4 steps inward of c, with their tabled taps.
+            const float *tz = b.taps + (long long)sample * kTapPlanes * g.fstride;
+            const float *tx = tz + (long long)kBandX * g.fstride;
+            const long long fs = g.fstride;
+            if (iz >= g.Lc && iz - 4 < g.pml) {  // top band, c = j - kk rows
 #pragma unroll
-                for (int d = 0; d < 4; ++d) {
-                    const int sz = d == 0 ? 1 : d == 1 ? -1 : 0, sx = d == 2 ? 1 : d == 3 ? -1 : 0;
+                for (int kk = 0; kk <= 4; ++kk) {
+                    const int cz = iz - kk;
+                    if (cz < g.Lc || cz >= g.pml) continue;
+                    const long long c = j - kk * P;
+                    if (kk < 3) out += __ldg(tz + kk * fs + c) * __ldg(lam1 + c);
+                    out -= __ldg(tz + (3 + kk) * fs + c) * __ldg(lam2 + c);
+                }
+            }
+            if (iz < g.ntz - g.Lc && iz + 4 >= g.ntz - g.pml) {  // bottom band, c = j + kk rows
 #pragma unroll
-                    for (int kk = 0; kk <= 4; ++kk) {
-                        const int cz = iz - kk * sz, cx = ix - kk * sx;
-                        if (cz < 0 || cz >= g.ntz || cx < 0 || cx >= g.ntx) continue;
-                        const CellInfo c = cell_unpack(__ldg(b.cells + (long long)cz * g.ntx + cx));
-                        const float gam = c.dir[0] == d ? c.gam[0] : c.dir[1] == d ? c.gam[1] : 0.0f;
-                        if (gam == 0.0f) continue;
-                        const long long ci = (long long)cz * P + cx + g.xoff;
-                        const Taps t = taps_of(__ldg(vdt + ci) / g.dx);
-                        const float c1 = kk == 0 ? 2.0f * t.t11 : kk == 1 ? 2.0f * t.t12 : kk == 2 ? 2.0f * t.t13 : 0.0f;
-                        const float c0 = kk == 0   ? t.t11 * t.t11
-                                         : kk == 1 ? 2.0f * t.t11 * t.t12
-                                         : kk == 2 ? t.t12 * t.t12 + 2.0f * t.t11 * t.t13
-                                         : kk == 3 ? 2.0f * t.t12 * t.t13
-                                                   : t.t13 * t.t13;
-                        out += gam * (c1 * __ldg(lam1 + ci) - c0 * __ldg(lam2 + ci));
-                    }
+                for (int kk = 0; kk <= 4; ++kk) {
+                    const int cz = iz + kk;
+                    if (cz < g.ntz - g.pml || cz >= g.ntz - g.Lc) continue;
+                    const long long c = j + kk * P;
+                    if (kk < 3) out += __ldg(tz + kk * fs + c) * __ldg(lam1 + c);
+                    out -= __ldg(tz + (3 + kk) * fs + c) * __ldg(lam2 + c);
+                }
+            }
+            if (ix >= g.Lc && ix - 4 < g.pml) {  // left band, c = j - kk columns
+#pragma unroll
+                for (int kk = 0; kk <= 4; ++kk) {
+                    const int cx = ix - kk;
+                    if (cx < g.Lc || cx >= g.pml) continue;
+                    const long long c = j - kk;
+                    if (kk < 3) out += __ldg(tx + kk * fs + c) * __ldg(lam1 + c);
+                    out -= __ldg(tx + (3 + kk) * fs + c) * __ldg(lam2 + c);
+                }
+            }
+            if (ix < g.ntx - g.Lc && ix + 4 >= g.ntx - g.pml) {  // right band, c = j + kk columns
+#pragma unroll
+                for (int kk = 0; kk <= 4; ++kk) {
+                    const int cx = ix + kk;
+                    if (cx < g.ntx - g.pml || cx >= g.ntx - g.Lc) continue;
+                    const long long c = j + kk;
+                    if (kk < 3) out += __ldg(tx + kk * fs + c) * __ldg(lam1 + c);
+                    out -= __ldg(tx + (3 + kk) * fs + c) * __ldg(lam2 + c);
                 }
             }
         }
@@ -285,21 +329,20 @@ __global__ void __launch_bounds__(kAdjThreads)
         nu0[j] = abv[q] * out;
         if (out == 0.0f) continue;
 
-        // d p2_j / d v_j of step k-1
-        const float v = vdv[q] / g.dt;
+        // d p2_j / d v_j of step k-1 (v dt^2 = (v dt) dt, d s / d v = dt / dx)
         float d = 0.0f;
         if (cj.sten) {
-            const float *sp1 = s_p1 + (rr + H) * kBoxX + lane + kHaloX;
+            const float *sp1 = s_p1 + (rr + H) * kBoxX + sc;
             float lx = fd_weight<H>(0) * sp1[0], lz = lx;
 #pragma unroll
             for (int m = 1; m <= H; ++m) {
                 lx += fd_weight<H>(m) * (sp1[m] + sp1[-m]);
                 lz += fd_weight<H>(m) * (sp1[m * kBoxX] + sp1[-m * kBoxX]);
             }
-            d += cj.beta * 2.0f * v * g.dt * g.dt * (lx * rdx2 + lz * rdz2);
+            d += cj.beta * 2.0f * vdv[q] * g.dt * (lx * rdx2 + lz * rdz2);
         }
         if (cj.nb) {
-            const float s = vdv[q] / g.dx;
+            const float s = vdv[q] * g.rdx;
             const Taps t = taps_of(s);
             const float u11 = (2.0f * s - 3.0f) * 0.5f, u12 = 2.0f - 2.0f * s, u13 = (2.0f * s - 1.0f) * 0.5f;
             for (int bb = 0; bb < cj.nb; ++bb) {
@@ -309,10 +352,10 @@ __global__ void __launch_bounds__(kAdjThreads)
                                  2.0f * (t.t12 * u12 + u11 * t.t13 + t.t11 * u13) * p0[j + 2 * sp] -
                                  2.0f * (u12 * t.t13 + t.t12 * u13) * p0[j + 3 * sp] -
                                  2.0f * t.t13 * u13 * p0[j + 4 * sp];
-                d += cj.gam[bb] * dE * g.dt / g.dx;
+                d += cj.gam[bb] * dE * b.dtdx;
             }
         }
-        if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * g.dt * v;
+        if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * vdv[q];
         b.gpad[(long long)inst * g.fstride + j] += out * d;
     }
 }

@@ -93,6 +93,7 @@ struct Batch {
     int inst0;           // first solve of this wave
     int slot0;           // first resident slot of this launch (the wave's second half)
     int levels;          // fields per resident slot of `ring`: 3, or the levels of a stored segment
+    int tm_slot0;        // resident slot of ring[0] in the tensor map's fields (a map over several rings)
     int imaging;         // run_fwi == 0
     int store;           // forward pass stores the wavefield for the adjoint
     double *spec;        // pseudo-spectral mode: [resident][ntz][ntx] real array, then the
@@ -555,7 +556,7 @@ __device__ __forceinline__ void step_tile(const CUtensorMap *tm_p1, const Geom &
     grid_launch_dependents();
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&bar, TS::kBytes);
-        tma_load_3d(s1, tm_p1, &bar, col0 - kHaloX, row0 - H, slot * b.levels + b1);
+        tma_load_3d(s1, tm_p1, &bar, col0 - kHaloX, row0 - H, (b.tm_slot0 + slot) * b.levels + b1);
     }
 
     WarpCtx w;
@@ -624,69 +625,98 @@ __global__ void __launch_bounds__(kThreads, MINB)
     step_tile<H, ADJ, U>(&tm_p1, g, b, sa, blockIdx.x, blockIdx.y, smem);
 }
 
-// One piece of a fused launch over instances of different geometry
-// (gb_fwi2d_run_instances): consecutive solves of one instance, with that
-// instance's geometry, buffers (the ring and stored field of these solves,
-// b.inst0 the first one) and Ricker table, the tensor map over their ring,
-// and where their blocks start in the launch.  Kept in device memory, 64-byte
-// aligned for the tensor map.
-struct __align__(64) InstanceStep {
-    CUtensorMap tm;        // the instance's ring, as k_step's tm_p1
-    Geom g;
-    Batch b;
-    const float *rik;      // [nt] Ricker wavelet (device)
-    int nres;              // its solves (resident slots 0..nres-1 of its ring)
-    int first_block;       // its first block in a launch (also in the launch's prefix array)
+// Fused launches over instances of different geometry (gb_fwi2d_run_instances).
+constexpr int kMaxPieces = 16;  // pieces per k_step_multi launch
+
+// One piece: consecutive solves of one instance -- its buffers (the ring and
+// stored field of these solves), acquisition and time axis, and where its
+// solves and blocks start.
+struct PieceArgs {
+    const float *vdt, *vel, *obs, *rik;
+    float *syn, *ring, *psave, *gacc;
+    int s_iz, r_iz, r_ix0, dr, nr, ds, s_ix0, ns, nt, nti, nt_save;
+    int inst0;        // its first solve within the instance
+    int tm_slot0;     // its first ring slot among the tensor map's fields
+    int nres;         // its solves
+    int first_block;  // its first block in the launch
 };
 
-// Shared memory of k_step_multi: the tile of k_step, then the block's copy of
-// its instance's geometry and buffers (read throughout the sweep).
-template <int H>
-struct MultiShape {
-    static constexpr int kGeomOff = (TileShape<H>::kSmem + 15) / 16 * 16;
-    static constexpr int kBatchOff = kGeomOff + (int)((sizeof(Geom) + 15) / 16 * 16);
-    static constexpr int kSmem = kBatchOff + (int)sizeof(Batch);
+// Everything a k_step_multi launch reads about its pieces, passed by value
+// as the kernel's parameter: the pieces share their grid (every Geom field
+// but the acquisition and the time axis) and their rings lie back to back
+// under one tensor map.  NP: the pieces it can hold (a launch's parameter
+// bytes are part of its fixed cost, so small launches take a small table).
+template <int NP>
+struct MultiArgsN {
+    CUtensorMap tm;
+    Geom gc;
+    const BlendCoef *coef;
+    int *status;
+    int blend_fp32, imaging, store, npieces;
+    int first[NP + 1];  // first blocks, ascending; first[npieces] = the blocks of all pieces
+    PieceArgs piece[NP];
 };
+using MultiArgs = MultiArgsN<kMaxPieces>;
 
-// One time step k of the first `nact` pieces of a wave (sorted by nt,
+// One time step k of the first `nact` pieces of a launch (sorted by nt,
 // longest first, so the pieces still running at step k are a prefix):
-// block -> piece by binary search of first[] (each piece's first block,
-// ascending), then (solve, tile) as in k_step.  Each piece's time index,
-// snapshot index and Ricker value follow from its own nt and nt_interval.
-template <int H, bool ADJ, int U, int MINB>
+// block -> piece by binary search of first[], then (solve, tile) as in
+// k_step.  All of it comes from the parameter space, as k_step's geometry
+// and buffers do: the grid's fields stay constant operands of the sweeps and
+// a piece's are constant-bank loads, which nothing the kernel stores can
+// alias.  Each piece's time index, snapshot index and Ricker value follow
+// from its own nt and nt_interval.
+template <int H, bool ADJ, int U, int MINB, int NP>
 __global__ void __launch_bounds__(kThreads, MINB)
-    k_step_multi(const InstanceStep *__restrict__ inst, const int *__restrict__ first, int nact, int k)
+    k_step_multi(const __grid_constant__ MultiArgsN<NP> a, int nact, int k)
 {
-    using MS = MultiShape<H>;
     extern __shared__ __align__(1024) float smem[];
-    Geom &g = *reinterpret_cast<Geom *>(reinterpret_cast<char *>(smem) + MS::kGeomOff);
-    Batch &b = *reinterpret_cast<Batch *>(reinterpret_cast<char *>(smem) + MS::kBatchOff);
     int lo = 0, hi = nact - 1;  // the last piece whose first block is <= blockIdx.x
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(first + mid) <= (int)blockIdx.x)
+        if (a.first[mid] <= (int)blockIdx.x)
             lo = mid;
         else
             hi = mid - 1;
     }
-    const InstanceStep &d = inst[lo];
-    // the piece's geometry and buffers into shared memory
-    static_assert(sizeof(Geom) % 4 == 0 && sizeof(Batch) % 4 == 0, "word copies");
-    const int *gs = reinterpret_cast<const int *>(&d.g);
-    const int *bs = reinterpret_cast<const int *>(&d.b);
-    int *gd = reinterpret_cast<int *>(&g), *bd = reinterpret_cast<int *>(&b);
-    for (int w = threadIdx.x; w < (int)(sizeof(Geom) / 4); w += kThreads) gd[w] = gs[w];
-    for (int w = threadIdx.x; w < (int)(sizeof(Batch) / 4); w += kThreads) bd[w] = bs[w];
-    __syncthreads();
+    const PieceArgs &pc = a.piece[lo];
+    Geom g = a.gc;
+    g.s_iz = pc.s_iz;
+    g.r_iz = pc.r_iz;
+    g.r_ix0 = pc.r_ix0;
+    g.dr = pc.dr;
+    g.nr = pc.nr;
+    g.ds = pc.ds;
+    g.s_ix0 = pc.s_ix0;
+    g.ns = pc.ns;
+    g.nt = pc.nt;
+    g.nti = pc.nti;
+    g.nt_save = pc.nt_save;
+    Batch b;
+    b.vdt = pc.vdt;
+    b.vel = pc.vel;
+    b.obs = pc.obs;
+    b.syn = pc.syn;
+    b.ring = pc.ring;
+    b.psave = pc.psave;
+    b.gacc = pc.gacc;
+    b.coef = a.coef;
+    b.blend_fp32 = a.blend_fp32;
+    b.status = a.status;
+    b.inst0 = pc.inst0;
+    b.slot0 = 0;
+    b.levels = 3;
+    b.tm_slot0 = pc.tm_slot0;
+    b.imaging = a.imaging;
+    b.store = a.store;
+    b.spec = nullptr;
+    b.kk = nullptr;
+    b.spec_resident = 0;
     const int it = ADJ ? g.nt - 1 - k : k;
-    const StepArgs sa = ring_step(k, it, (it % g.nti) == 0 ? it / g.nti : -1, ADJ ? 0.0f : __ldg(d.rik + it));
-    // The tensor map was copied to device memory before the launch: order
-    // that copy before the asynchronous proxy reads it.
-    if (threadIdx.x == 0)
-        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&d.tm) : "memory");
-    const int local = (int)blockIdx.x - d.first_block;
-    const int rank = local / d.nres;
-    step_tile<H, ADJ, U>(&d.tm, g, b, sa, local - rank * d.nres, rank, smem);
+    const StepArgs sa = ring_step(k, it, (it % g.nti) == 0 ? it / g.nti : -1, ADJ ? 0.0f : __ldg(pc.rik + it));
+    const int local = (int)blockIdx.x - pc.first_block;
+    const int rank = local / pc.nres;
+    step_tile<H, ADJ, U>(&a.tm, g, b, sa, local - rank * pc.nres, rank, smem);
 }
 
 }  // namespace gbfwi

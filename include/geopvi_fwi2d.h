@@ -142,8 +142,9 @@ size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, 
  * geopvi/forward/fwi2d/posterior.py:112-149 for callers whose samples belong
  * to different inversions.
  *
- * Fused (flags without GB_FWI2D_PLAIN, CHECKPOINT, EXACT_GRADIENT, GRAPH or a
- * forced variant; finite-difference instances): the solves of all instances
+ * Fused (flags without GB_FWI2D_PLAIN, CHECKPOINT, EXACT_GRADIENT or GRAPH;
+ * finite-difference instances; GB_FWI2D_VARIANT does not apply): the solves
+ * of all instances
  * of one FD order are packed, longest nt first, into waves that fill
  * work_bytes (at most max_resident solves each when max_resident > 0), and a
  * wave advances all its solves -- of any grid, acquisition and time axis --

@@ -129,7 +129,7 @@ def _fused_setup(cuda, names, flags, syn_none=()):
                                        ptr(out[2])))
         keep.append((vel, obs, out))
         alone.append((p, n, vel, obs, ref))
-        nts[name] = (p.Lc, p.nt, n)
+        nts[name] = ((p.Lc, p.nz, p.nx, p.pml0, p.dx, p.dz, p.dt), p.nt)
     return stream, insts, keep, alone, nts
 
 
@@ -172,12 +172,13 @@ def test_fused_waves_match_single_batches(engine_lib, cuda, room, max_resident, 
                 assert torch.equal(a, b)
     if room == "all" and max_resident == 0:
         # one wave per FD order: per instance k_prepare, the reduction and the
-        # misfit's two kernels; per order one launch per step and pass
+        # misfit's two kernels; per grid one launch per step and pass while
+        # one of its instances runs
         fwd_only = bool(flags & _native.FLAG_FORWARD_ONLY)
-        by_order = {}
-        for lc, nt, _ in nts.values():
-            by_order[lc] = max(by_order.get(lc, 0), nt)
-        expect = len(insts) * (1 + (0 if fwd_only else 1) + 2) + sum(by_order.values()) * (1 if fwd_only else 2)
+        by_grid = {}
+        for key, nt in nts.values():
+            by_grid[key] = max(by_grid.get(key, 0), nt)
+        expect = len(insts) * (1 + (0 if fwd_only else 1) + 2) + sum(by_grid.values()) * (1 if fwd_only else 2)
         assert engine_lib.gb_fwi2d_last_launch_count() == expect
 
 
@@ -203,3 +204,39 @@ def test_fused_wave_plan(engine_lib):
     big = [instance(p) for p in workloads.cfg4_instances()]
     arr = (_native.CInstance * len(big))(*big)
     assert 10 <= engine_lib.gb_fwi2d_instances_waves(arr, len(big), 0, 0, 150 << 30) <= 20
+
+
+@pytest.mark.gpu
+def test_fused_halves_on_two_streams(engine_lib, cuda):
+    """Two instances of one grid with 51 solves in one wave: the launch runs
+    as two halves on two streams, cutting the first instance's piece at solve
+    25 -- results still those of each instance alone."""
+    import torch
+    names = ("fwi_o8", "fwi_o8_nti2")
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    insts, keep, alone = [], [], []
+    for name, n in zip(names, (12, 5)):
+        z = np.load(os.path.join(GOLDEN, name + ".npz"))
+        p = cases.params_from_npz(z)
+        vels = np.stack([z["start"] * np.float32(1 + 0.005 * i) for i in range(n)]).astype(np.float32)
+        vel = torch.from_numpy(vels).to(cuda)
+        obs = torch.from_numpy(np.ascontiguousarray(z["obs"], dtype=np.float32)).to(cuda)
+        out = (torch.full((n, p.data_len), -1.0, device=cuda), torch.full((n, p.ncell), -1.0, device=cuda),
+               torch.full((n,), -1.0, dtype=torch.float64, device=cuda))
+        insts.append(_native.CInstance(p.c(), n, vel.data_ptr(), obs.data_ptr(), out[0].data_ptr(),
+                                       out[1].data_ptr(), out[2].data_ptr()))
+        keep.append((vel, obs, out))
+        alone.append((p, n, vel, obs, tuple(torch.empty_like(t) for t in out)))
+    _run_alone(engine_lib, cuda, alone, 0, stream)
+    arr = (_native.CInstance * 2)(*insts)
+    nbytes = sum(engine_lib.gb_fwi2d_workspace_bytes(ctypes.byref(p.c()), n, 0, 0) for p, n, *_ in alone) + (8 << 20)
+    assert engine_lib.gb_fwi2d_instances_waves(arr, 2, 0, 0, nbytes) == 1
+    work = torch.empty(nbytes, dtype=torch.uint8, device=cuda)
+    assert engine_lib.gb_fwi2d_run_instances(arr, 2, 0, 0, work.data_ptr(), nbytes, stream) == 0
+    torch.cuda.synchronize(cuda)
+    assert engine_lib.gb_fwi2d_status(ctypes.c_void_p(work.data_ptr()), ctypes.c_void_p(stream)) == 0
+    for (_, _, out), (*_, ref) in zip(keep, alone):
+        for a, b in zip(out, ref):
+            assert torch.equal(a, b)
+    # two launches per step while both halves run: fwi_o8's 300 steps, fwi_o8_nti2's 301
+    assert engine_lib.gb_fwi2d_last_launch_count() == 2 * (1 + 1 + 2) + 2 * (300 + 301)
