@@ -646,12 +646,15 @@ def run_uneven(args):
         for name, p, _, obs in jobs:
             srv.register(name, p, obs)
         torch.cuda.synchronize(dev)
+        sampler = ClockSampler(dev.index or 0)
+        sampler.start()
         t0 = time.perf_counter()
         futs = srv.submit_many([(name, vel) for name, _, vel, _ in jobs])
         for k, f in enumerate(futs):
             f.result(timeout=600)
             print(f"cfg4: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
+        clocks = sampler.stop()
     print(json.dumps({
         "metric": "FD cell-updates/s (misfit+gradient, fwd+adjoint)", "value": cells / wall,
         "unit": "cell-updates/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
@@ -662,7 +665,7 @@ def run_uneven(args):
                    "instances": len(jobs), "cell_updates": cells,
                    "storage": "one fused gb_fwi2d_run_instances call: full storage, waves of mixed instances",
                    "hbm_budget_gb": budget / (1 << 30)},
-        "sample_gradients_per_s": len(jobs) / wall,
+        "sample_gradients_per_s": len(jobs) / wall, "clocks": clocks,
         "e2e": {"value": cells / wall, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(sum(v.nbytes for _, _, v, _ in jobs)),
                 "d2h_bytes_per_step": int(sum(8 + 4 * p.ncell for _, p, _, _ in jobs)),

@@ -905,22 +905,36 @@ static long long enqueue_checkpointed(const Call &c, Batch b, int nres, cudaStre
     return launches;
 }
 
+// overlap: the previous operation on `st` is a step kernel, and this one may
+// be launched programmatically (it waits for that step before reading
+// anything the step writes).
 template <int H>
 static void launch_adjoint_exact(const Call &c, const ExactBatch &x, int nres, int k, int lev1, float rik,
-                                 cudaStream_t st)
+                                 cudaStream_t st, bool overlap)
 {
     const Geom &g = c.d->g;
-    const dim3 grid((unsigned)(g.tiles_x * g.tiles_z), nres);
-    k_adjoint_tile<H><<<grid, kAdjThreads, AdjShape<H>::kSmem, st>>>(c.maps3.p1, c.maps2.p1, g, x, k, lev1, rik);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(g.tiles_x * g.tiles_z), nres);
+    cfg.blockDim = dim3(kAdjThreads);
+    cfg.dynamicSmemBytes = AdjShape<H>::kSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlap ? 1 : 0;
+    if (cudaLaunchKernelEx(&cfg, k_adjoint_tile<H>, c.maps3.p1, c.maps2.p1, g, x, k, lev1, rik) != cudaSuccess)
+        t_enqueue_error = GB_FWI2D_ECUDA;
 }
 
-static void adjoint_exact(const Call &c, const ExactBatch &x, int nres, int k, int lev1, float rik, cudaStream_t st)
+static void adjoint_exact(const Call &c, const ExactBatch &x, int nres, int k, int lev1, float rik, cudaStream_t st,
+                          bool overlap)
 {
     switch (c.d->g.Lc - 1) {
-    case 3: launch_adjoint_exact<3>(c, x, nres, k, lev1, rik, st); break;
-    case 4: launch_adjoint_exact<4>(c, x, nres, k, lev1, rik, st); break;
-    case 5: launch_adjoint_exact<5>(c, x, nres, k, lev1, rik, st); break;
-    default: launch_adjoint_exact<6>(c, x, nres, k, lev1, rik, st); break;
+    case 3: launch_adjoint_exact<3>(c, x, nres, k, lev1, rik, st, overlap); break;
+    case 4: launch_adjoint_exact<4>(c, x, nres, k, lev1, rik, st, overlap); break;
+    case 5: launch_adjoint_exact<5>(c, x, nres, k, lev1, rik, st, overlap); break;
+    default: launch_adjoint_exact<6>(c, x, nres, k, lev1, rik, st, overlap); break;
     }
 }
 
@@ -994,18 +1008,23 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
     x.rdz2 = 1.0f / (g.dz * g.dz);
     x.dtdx = g.dt / g.dx;
 
+    // prev_step: the last operation enqueued on st is a step kernel, so the
+    // next may be launched programmatically.
+    bool prev_step = false;
     // step it with p0 = store level l, p1 = l + 1, p2 = l + 2
     auto fwd_store = [&](int it, int l, int nres) {
         StepArgs sa = ring_step(it, it, -1, c.d->rik[it]);
         sa.l0 = l;
         sa.l1 = l + 1;
         sa.l2 = l + 2;
-        launches += step(false, c.maps2, g, bs, nres, sa, st, c.variant);
+        launches += step(false, c.maps2, g, bs, nres, sa, st, c.variant, prev_step);
+        prev_step = true;
     };
     const int wave = (c.flags & GB_FWI2D_PLAIN) ? 1 : L.resident;
     for (long long i0 = 0; i0 < ninst; i0 += wave) {
         const int nres = (int)std::min<long long>(wave, ninst - i0);
         b.inst0 = bs.inst0 = x.inst0 = (int)i0;
+        prev_step = false;
         if (nseg == 1) {  // every level in the store: P^-1 = P^0 = 0, step it writes level it + 2
             cudaMemset2DAsync(store, store_pitch, 0, 2 * fbytes, nres, st);
             for (int it = 0; it < g.nt; ++it) fwd_store(it, it, nres);
@@ -1018,23 +1037,29 @@ static long long enqueue_exact(const Call &c, cudaStream_t st)
                         cudaMemcpy2DAsync((char *)ck + (size_t)(2 * s + h) * fbytes, ck_pitch,
                                           (char *)ring + (size_t)((it + h) % 3) * fbytes, ring_pitch, fbytes, nres,
                                           cudaMemcpyDeviceToDevice, st);
+                    prev_step = false;
                 }
-                launches += step(false, c.maps, g, b, nres, ring_step(it, it, -1, c.d->rik[it]), st, c.variant);
+                launches += step(false, c.maps, g, b, nres, ring_step(it, it, -1, c.d->rik[it]), st, c.variant,
+                                 prev_step);
+                prev_step = true;
             }
         }
         // lambda^{nt+1} = lambda^{nt+2} = 0, and nu with them (its pad columns stay zero)
         cudaMemsetAsync(lam, 0, 3 * fbytes * (size_t)nres, st);
         cudaMemsetAsync(nu, 0, 3 * fbytes * (size_t)nres, st);
+        prev_step = false;
         for (int s = nseg - 1; s >= 0; --s) {
             const int i0s = s * K, i1s = std::min(i0s + K, g.nt);
             if (nseg > 1) {
                 // the pair (P^{i0s-1}, P^{i0s}) into store levels 0, 1; recompute the segment
                 cudaMemcpy2DAsync(store, store_pitch, (char *)ck + (size_t)(2 * s) * fbytes, ck_pitch, 2 * fbytes,
                                   nres, cudaMemcpyDeviceToDevice, st);
+                prev_step = false;
                 for (int it = i0s; it <= i1s - 2; ++it) fwd_store(it, it - i0s, nres);
             }
             for (int k = i1s; k >= i0s + 1; --k) {
-                adjoint_exact(c, x, nres, k, k - i0s, c.d->rik[k - 1], st);
+                adjoint_exact(c, x, nres, k, k - i0s, c.d->rik[k - 1], st, prev_step);
+                prev_step = true;
                 ++launches;
             }
         }

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
     using AS = AdjShape<H>;
     extern __shared__ __align__(1024) float smem[];
     float *s_nu = smem, *s_p1 = smem + AS::kTile;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(smem + 2 * AS::kTile);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * AS::kTile);  // [0] nu, [1] P^{k-1}
     const int slot = blockIdx.y;
     const int inst = b.inst0 + slot;
     const int sample = inst / g.ns, shot = inst - sample * g.ns;
@@ -197,15 +197,11 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
     const int col0 = tcol * kTileX, row0 = trow * kTileZ;
     const int lane = threadIdx.x & 31, rr0 = threadIdx.x >> 5;  // tile rows rr0 + q * RS
     if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         fence_barrier_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, AS::kBytes);
-        tma_load_3d(s_nu, &tm_nu, &bar, col0 - kHaloX, row0 - H, slot * 3 + (k + 1) % 3);
-        tma_load_3d(s_p1, &tm_store, &bar, col0 - kHaloX, row0 - H, slot * b.store_levels + lev1);
-    }
     const long long P = g.pitch;
     const float *vdt = b.vdt + (long long)sample * g.fstride;
     float *l_base = b.lam + (long long)slot * 3 * g.fstride;
@@ -224,7 +220,8 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
     const bool plain = ix0 >= g.pml + 4 && ix0 + kTileX <= g.ntx - g.pml - 4 && row0 >= g.pml + 4 &&
                        row0 + kTileZ <= g.ntz - g.pml - 4;
 
-    // Per cell: the first loads, issued while the tiles are in flight.
+    // The per-sample fields are constant through the call: read them while
+    // the previous step drains.
     const int ix = ix0 + lane;
     const bool col_live = ix >= 0 && ix < g.ntx;
     const long long j0 = (long long)(row0 + rr0) * P + col0 + lane;
@@ -232,23 +229,43 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         const bool live = col_live && row0 + rr0 + q * RS < g.ntz;
-        l1v[q] = live ? __ldg(lam1 + j0 + q * RS * P) : 0.0f;
-        l2v[q] = live ? __ldg(lam2 + j0 + q * RS * P) : 0.0f;
         abv[q] = live ? __ldg(ab + j0 + q * RS * P) : 0.0f;
         vdv[q] = live ? __ldg(vdt + j0 + q * RS * P) : 0.0f;
     }
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
-        mbar_wait_bounded(&bar, 0);  // the copies may still land: wait again (bounded) before retiring
-        return;
+    // Below here every read may see the previous step's writes (lambda^{k+1},
+    // nu^{k+1}, the gradient accumulator): launched programmatically, this
+    // step waits for it first.
+    grid_dependency_wait();
+    grid_launch_dependents();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar[0], AS::kBytes / 2);
+        tma_load_3d(s_nu, &tm_nu, &bar[0], col0 - kHaloX, row0 - H, slot * 3 + (k + 1) % 3);
+        mbar_arrive_expect_tx(&bar[1], AS::kBytes / 2);
+        tma_load_3d(s_p1, &tm_store, &bar[1], col0 - kHaloX, row0 - H, slot * b.store_levels + lev1);
     }
-    if (!col_live) return;
-    const int sc = lane + kHaloX;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
+        const bool live = col_live && row0 + rr0 + q * RS < g.ntz;
+        l1v[q] = live ? lam1[j0 + q * RS * P] : 0.0f;
+        l2v[q] = live ? lam2[j0 + q * RS * P] : 0.0f;
+    }
+    if (!mbar_wait_bounded(&bar[0], 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        // the copies may still land: wait again (bounded) for both before retiring
+        mbar_wait_bounded(&bar[0], 0);
+        mbar_wait_bounded(&bar[1], 0);
+        return;
+    }
+    const int sc = lane + kHaloX;
+    float outv[R];
+    int4 cpk[R];  // each row's cell facts, packed (cell_pack)
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        outv[q] = 0.0f;
+        if (!col_live) continue;
         const int rr = rr0 + q * RS;
         const int iz = row0 + rr;
-        if (iz >= g.ntz) break;
+        if (iz >= g.ntz) continue;
         const long long j = j0 + q * RS * P;
         const float *sn = s_nu + (rr + H) * kBoxX + sc;  // nu^{k+1} at j in the tile
         float out = 0.0f;
@@ -327,7 +344,25 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
         }
         lam0[j] = out;
         nu0[j] = abv[q] * out;
+        outv[q] = out;
+        cpk[q] = cell_pack(cj);
+    }
+    // Every thread waits for the second tile, so the block retires only after
+    // its copy has landed.
+    if (!mbar_wait_bounded(&bar[1], 0)) {
+        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+        mbar_wait_bounded(&bar[1], 0);
+        return;
+    }
+    if (!col_live) return;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        const float out = outv[q];
         if (out == 0.0f) continue;
+        const int rr = rr0 + q * RS;
+        const int iz = row0 + rr;
+        const long long j = j0 + q * RS * P;
+        const CellInfo cj = cell_unpack(cpk[q]);
 
         // d p2_j / d v_j of step k-1 (v dt^2 = (v dt) dt, d s / d v = dt / dx)
         float d = 0.0f;

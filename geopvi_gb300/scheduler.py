@@ -5,11 +5,12 @@ another (geopvi/forward/fwi2d/posterior.py:112-149).  This module serves many
 such evaluations at once: requests from several inversions (each with its own
 grid, acquisition, time axis and observed data) arrive at any time; a
 dispatcher thread admits them as HBM and streams free up and merges queued
-requests of the same inversion into one batch.  When several inversions are
-queued, their batches go to the engine in one gb_fwi2d_run_instances call,
-whose waves mix solves of different geometry in one launch per time step;
-a lone batch chooses how it holds its forward field (full storage in waves,
-or sqrt(nt) checkpoints) from a cost model.  Admitted calls run
+requests of the same inversion into one batch.  Batches of several
+inversions submitted together (submit_many) go to the engine in one
+gb_fwi2d_run_instances call, whose waves mix solves of different geometry in
+one launch per time step, when the cost model expects that to be faster than
+their own plans; every other batch chooses how it holds its forward field
+(full storage in waves, or sqrt(nt) checkpoints) from the cost model.  Admitted calls run
 concurrently on a pool of CUDA streams.  Observed data stay resident per
 inversion; each call's workspace lives only while it runs.
 
@@ -51,6 +52,24 @@ def step_seconds(p: Params, resident: int) -> float:
     """Estimated time of one time step of a wave of `resident` solves."""
     strip = 1.0 - (p.nx * p.nz) / p.ntp
     return LAUNCH_OVERHEAD_S + resident * p.ntp * (CELL_S + STRIP_CELL_S * strip)
+
+
+def fused_seconds(batches: list, cap_bytes: int, lib=None) -> float:
+    """Estimated time of one fused gb_fwi2d_run_instances call over
+    `batches` [(Params, nsamples)] in cap_bytes: every step of every solve
+    (full storage, 2 nt steps) at the step kernel's per-cell cost, plus the
+    launches -- a wave's launch serves all its solves, so a pass costs about
+    one launch per step of the longest time axis, and the waves are the
+    stored fields over the workspace (each batch's nt weighted by its share)."""
+    lib = lib or _native.load()
+    work = wave_steps = 0.0
+    longest = 0
+    for p, n in batches:
+        strip = 1.0 - (p.nx * p.nz) / p.ntp
+        work += 2 * p.nt * n * p.ns * p.ntp * (CELL_S + STRIP_CELL_S * strip)
+        wave_steps += p.nt * _ws(lib, p.c(), n, 0, 0) / cap_bytes
+        longest = max(longest, p.nt)
+    return work + 2 * max(wave_steps, longest) * LAUNCH_OVERHEAD_S
 
 
 @dataclass
@@ -137,6 +156,7 @@ class Request:
     inversion: str
     vel: torch.Tensor                  # (n, nz*nx) float32, host or device
     want_syn: bool = False
+    together: bool = False             # came with others through submit_many
     future: Future = field(default_factory=Future)
     t_submit: float = 0.0
     t_start: float = 0.0
@@ -231,6 +251,8 @@ class FwiServer:
     def submit_many(self, items, want_syn: bool = False) -> list:
         """Submit [(name, vel), ...] at once: the dispatcher sees all of them together."""
         reqs = [self._request(name, vel, want_syn) for name, vel in items]
+        for r in reqs:
+            r.together = True
         self._queue.put(reqs)
         return [r.future for r in reqs]
 
@@ -357,18 +379,26 @@ class FwiServer:
 
     def _fused_call(self, groups: list, cap: int):
         """The groups (one imaging mode) that one gb_fwi2d_run_instances call
-        runs in `cap` bytes, and its workspace size; None if fewer than two fit."""
+        runs in `cap` bytes, and its workspace size; None if fewer than two fit
+        or if the cost model prefers the batches one by one (full storage only:
+        where the stored fields dwarf the workspace, waves of a few solves
+        cost more than the batches' own plans, which may checkpoint)."""
         imaging = self._inv[groups[0][0]].imaging
         groups = [g for g in groups if self._inv[g[0]].imaging == imaging]
+        flags = _native.FLAG_IMAGING if imaging else 0
         while len(groups) > 1:
             insts = (_native.CInstance * len(groups))(*[
                 _native.CInstance(self._inv[name].params.c(), n, 1, 1, None, 1, None) for name, _, n in groups])
-            flags = _native.FLAG_IMAGING if imaging else 0
             need = int(self.lib.gb_fwi2d_instances_workspace_bytes(insts, len(groups), 0, flags))
             if 0 < need <= cap:
-                # room for every solve resident at once, capped by the arena
-                full = sum(_ws(self.lib, self._inv[name].params.c(), n, 0, flags) for name, _, n in groups)
-                return groups, int(min(cap, full + (8 << 20)))
+                batches = [(self._inv[name].params, n) for name, _, n in groups]
+                alone = [plan_batch(p, n, cap, self.lib) for p, n in batches]
+                if any(a is None for a in alone) or fused_seconds(batches, cap, self.lib) <= sum(
+                        a.est_seconds for a in alone):
+                    # room for every solve resident at once, capped by the arena
+                    full = sum(_ws(self.lib, p.c(), n, 0, flags) for p, n in batches)
+                    return groups, int(min(cap, full + (8 << 20)))
+                return None
             groups = groups[:-1]
         return None
 
@@ -379,7 +409,8 @@ class FwiServer:
             free = self._arena.largest()
             # a call may take all of the free arena when it runs alone, half otherwise
             cap = free if not self._running else free // 2
-            fused = self._fused_call(groups, cap) if len(groups) > 1 else None
+            together = [g for g in groups if all(r.together for r in g[1])]
+            fused = self._fused_call(together, cap) if len(together) > 1 else None
             if fused is not None:
                 sel, nbytes = fused
                 for _, reqs, _ in sel:

@@ -231,3 +231,19 @@ def test_server_merges_queued_requests_per_inversion():
     assert [(name, [r.nsamples for r in reqs], n) for name, reqs, n in groups] == [
         ("a", [3, 4], 7), ("b", [2, 1], 3), ("c", [9], 9)]
     assert np.sum([n for *_, n in groups]) == 19
+
+
+def test_fused_call_chosen_by_cost():
+    """Many small instances (the uneven batch of 48) fuse; a few requests
+    whose full storage is ~100x the workspace run their own, checkpointed
+    plans instead (the fused call would run waves of a few solves)."""
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import fused_seconds, plan_batch
+    cap = 150 << 30
+    uneven = [(p, 1) for p in workloads.cfg4_instances()]
+    alone = sum(plan_batch(p, n, cap).est_seconds for p, n in uneven)
+    assert fused_seconds(uneven, cap) < 0.8 * alone
+    big = [(workloads.make_params(400, 800, 5000, 1e-3, 40, 8.0), 32),
+           (workloads.make_params(300, 600, 4500, 1e-3, 30, 8.0), 24)]
+    alone = sum(plan_batch(p, n, cap // 2).est_seconds for p, n in big)
+    assert fused_seconds(big, cap // 2) > alone
