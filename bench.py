@@ -692,11 +692,11 @@ def _serve(dev, inv, reqs, gaps, label):
                 time.sleep(delay)
             futs.append(srv.submit(name, vel))
         t_arrivals = time.perf_counter() - t0
+        print(f"cfg5 {label}: {len(futs)} requests submitted in {t_arrivals:.1f} s", file=sys.stderr, flush=True)
         for k, f in enumerate(futs):
             f.result(timeout=3600)
-            if (k + 1) % 20 == 0:
-                print(f"cfg5 {label}: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s",
-                      file=sys.stderr, flush=True)
+            print(f"cfg5 {label}: {k + 1}/{len(futs)} done at {time.perf_counter() - t0:.1f} s",
+                  file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
         clocks = sampler.stop()
         lat = latency_summary(srv.completed)
@@ -738,6 +738,7 @@ def run_serving(args):
         vel = (base[None] + rng.normal(0.0, 60.0, (n,) + base.shape)).reshape(n, -1).astype(np.float32)
         reqs.append((name, p, vel))
     unit_gaps = rng.exponential(1.0, len(reqs))  # Poisson arrivals, scaled per load
+    print(f"cfg5: {len(inv)} inversions registered, {len(reqs)} requests drawn", file=sys.stderr, flush=True)
     over = _serve(dev, inv, reqs, unit_gaps / args.rate, f"{args.rate} req/s")
     capacity = over["requests_per_s"]  # the server is busy throughout: its throughput is the capacity
     rate2 = args.below_saturation * capacity

@@ -46,7 +46,7 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".inc"))]
     deps += [os.path.join(REPO_DIR, "include", h) for h in ("geopvi_fwi2d.h", "geopvi_fwi3d.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 

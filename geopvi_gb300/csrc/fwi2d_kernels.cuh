@@ -505,113 +505,6 @@ __device__ __forceinline__ void sweep_general(const Geom &g, const Batch &b, con
 // boundary's p0 neighbours hit L1/L2), which keeps shared memory at ~4.6 KB
 // per block.  The warp then sweeps its 16 rows with the interior or the
 // general row body, a warp-uniform choice.
-// One (solve, tile) of a step: the body of k_step and of k_step_multi.  The
-// tile rank visits tile rows and columns from the edges inward, so the tiles
-// with absorbing strips (the longest) of every solve are dispatched first and
-// each launch ends on interior tiles: a short tail before the next step.
-// `smem` is the block's dynamic shared memory, 1024-byte aligned.
-template <int H, bool ADJ, int U>
-__device__ __forceinline__ void step_tile(const CUtensorMap *tm_p1, const Geom &g, const Batch &b,
-                                          const StepArgs &sa, int solve, int rank, float *smem)
-{
-    using TS = TileShape<H>;
-    float *s1 = smem;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(s1 + TS::kP1Floats);
-
-    const int slot = b.slot0 + solve;
-    const int rr = rank / g.tiles_x, cr = rank - rr * g.tiles_x;
-    const int trow = (rr & 1) ? g.tiles_z - 1 - (rr >> 1) : (rr >> 1);
-    const int tcol = (cr & 1) ? g.tiles_x - 1 - (cr >> 1) : (cr >> 1);
-    const int col0 = tcol * kTileX;
-    const int row0 = trow * kTileZ;
-    const int b0 = sa.l0, b1 = sa.l1, b2 = sa.l2;
-
-    // Tiles with no column in [Lc, ntx - Lc): the rim, which neither the
-    // stencil nor abc_for_p's passes change from its initial zero (the top and
-    // bottom passes blend rim columns from rim neighbours only), so the new
-    // level is zero there.  Block-uniform; no staging.
-    if (col0 - g.xoff + kTileX <= g.Lc || col0 - g.xoff >= g.ntx - g.Lc) {
-        grid_dependency_wait();
-        grid_launch_dependents();
-        const int ix = col0 - g.xoff + (threadIdx.x & 31);
-        if (ix >= 0 && ix < g.ntx) {
-            float *p2 = b.ring + ((long long)slot * b.levels + b2) * g.fstride + col0 + (threadIdx.x & 31);
-            const int iz0 = row0 + (threadIdx.x >> 5) * kWarpRows;
-#pragma unroll 4
-            for (int j = 0; j < kWarpRows; ++j)
-                if (iz0 + j < g.ntz) p2[(long long)(iz0 + j) * g.pitch] = 0.0f;
-        }
-        return;
-    }
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    // Everything above touched no global memory; the previous step (which
-    // writes p1 and reads the buffer p2 overwrites) must be complete below.
-    // Its successor may be scheduled once every block of this one is past here.
-    grid_dependency_wait();
-    grid_launch_dependents();
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, TS::kBytes);
-        tma_load_3d(s1, tm_p1, &bar, col0 - kHaloX, row0 - H, (b.tm_slot0 + slot) * b.levels + b1);
-    }
-
-    WarpCtx w;
-    w.inst = b.inst0 + slot;
-    w.sample = w.inst / g.ns;
-    w.shot = w.inst - w.sample * g.ns;
-    w.lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int col = col0 + w.lane;
-    w.ix = col - g.xoff;
-    w.cx = w.lane + kHaloX;
-    w.rr0 = warp * kWarpRows;
-    w.iz0 = row0 + w.rr0;
-    w.s1 = s1;
-    const bool live = w.ix >= 0 && w.ix < g.ntx;
-    float *ring = b.ring + (long long)slot * b.levels * g.fstride;
-    w.p0 = ring + (long long)b0 * g.fstride;
-    w.p2 = ring + (long long)b2 * g.fstride;
-    w.vdt = b.vdt + (long long)w.sample * g.fstride;
-    w.c = (long long)w.iz0 * g.pitch + col;
-
-    // Issue this thread's first p0 / v*dt loads while the tile is in flight.
-    float p0_next = 0.0f, vd_next = 0.0f;
-    if (live && w.iz0 < g.ntz) {
-        p0_next = __ldg(w.p0 + w.c);
-        vd_next = __ldg(w.vdt + w.c);
-    }
-
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
-        // The copy may still land in this block's shared memory: wait for it
-        // a second time (bounded) before the block retires.
-        mbar_wait_bounded(&bar, 0);
-        return;
-    }
-    if (!live || w.iz0 >= g.ntz) return;
-
-    const bool inner_x = w.ix >= g.pml && w.ix < g.ntx - g.pml;
-    w.ps = nullptr;
-    w.G = nullptr;
-    if (sa.snap >= 0 && inner_x && (ADJ || b.store)) {
-        w.ps = b.psave + ((long long)slot * g.nt_save + sa.snap) * g.pstride + (w.ix - g.pml + g.ioff);
-        if (ADJ) w.G = b.gacc + (long long)w.inst * g.pstride + (w.ix - g.pml + g.ioff);
-    }
-    // Warp-uniform: all 16 rows and 32 columns interior, no source or receiver row.
-    const int ix0 = col0 - g.xoff;
-    const bool cols_interior = ix0 >= g.pml && ix0 + kTileX <= g.ntx - g.pml;
-    const bool interior = cols_interior && w.iz0 >= g.pml && w.iz0 + kWarpRows <= g.ntz - g.pml &&
-                          (g.s_iz < w.iz0 || g.s_iz >= w.iz0 + kWarpRows) &&
-                          (g.r_iz < w.iz0 || g.r_iz >= w.iz0 + kWarpRows);
-    if (interior)
-        sweep_interior<H, ADJ, U>(g, b, sa, w, p0_next, vd_next);
-    else
-        sweep_general<H, ADJ>(g, b, sa, w, p0_next, vd_next);
-}
 
 // One time step of every solve in the wave, one block per (resident slot,
 // tile): blockIdx.x = solve, blockIdx.y = tile rank.
@@ -622,7 +515,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
     // Dynamic shared memory only (no static __shared__), so the tile starts
     // at the 1024-byte aligned base.
     extern __shared__ __align__(1024) float smem[];
-    step_tile<H, ADJ, U>(&tm_p1, g, b, sa, blockIdx.x, blockIdx.y, smem);
+    const CUtensorMap *tile_map = &tm_p1;
+    const int solve = blockIdx.x, rank = blockIdx.y;
+#include "fwi2d_step_tile.inc"
 }
 
 // Fused launches over instances of different geometry (gb_fwi2d_run_instances).
@@ -716,7 +611,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
     const StepArgs sa = ring_step(k, it, (it % g.nti) == 0 ? it / g.nti : -1, ADJ ? 0.0f : __ldg(pc.rik + it));
     const int local = (int)blockIdx.x - pc.first_block;
     const int rank = local / pc.nres;
-    step_tile<H, ADJ, U>(&a.tm, g, b, sa, local - rank * pc.nres, rank, smem);
+    const int solve = local - rank * pc.nres;
+    const CUtensorMap *tile_map = &a.tm;
+#include "fwi2d_step_tile.inc"
 }
 
 }  // namespace gbfwi

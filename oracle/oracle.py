@@ -22,6 +22,7 @@ from __future__ import annotations
 import ctypes
 import os
 import subprocess
+import sys
 import tempfile
 from dataclasses import dataclass, fields
 
@@ -116,7 +117,8 @@ def build() -> None:
     cmd = ["make", "-s", "-C", ORACLE_DIR, "all"]
     if os.path.isfile(os.path.join(REFERENCE_FWI2D, "fdtd2D_modelling.c")):
         cmd.append(f"REF_SRC={REFERENCE_FWI2D}")
-    subprocess.run(cmd, check=True)
+    # make's messages go to stderr: a bench run's stdout carries one JSON line
+    subprocess.run(cmd, check=True, stdout=sys.stderr)
 
 
 _lib = None
