@@ -257,6 +257,61 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks)
         return;
     }
     const int sc = lane + kHaloX;
+    if (plain) {
+        // Every cell a stencil cell with beta = 1 and no blend within reach:
+        // the same arithmetic as below with those facts as constants, and
+        // 32-bit offsets within the fields (a field is far below 2^31 cells).
+        const int jp = (row0 + rr0) * g.pitch + col0 + lane;
+        float outp[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const int rr = rr0 + q * RS;
+            const int iz = row0 + rr;
+            const int j = jp + q * RS * g.pitch;
+            const float *sn = s_nu + (rr + H) * kBoxX + sc;
+            float out = 0.0f;
+            if (iz == g.r_iz) {  // R^T r_{k-1}
+                const int ir = receiver_of(g, ix);
+                if (ir >= 0) {
+                    const long long t = (long long)(k - 1) * g.nr + ir;
+                    out += b.syn[(long long)inst * g.nt * g.nr + t] - b.obs[(long long)shot * g.nt * g.nr + t];
+                }
+            }
+            out += 2.0f * l1v[q] + fd_weight<H>(0) * (rdx2 + rdz2) * sn[0];
+            out -= l2v[q];
+#pragma unroll
+            for (int m = 1; m <= H; ++m)
+                out += fd_weight<H>(m) * (rdx2 * (sn[m] + sn[-m]) + rdz2 * (sn[m * kBoxX] + sn[-m * kBoxX]));
+            lam0[j] = out;
+            nu0[j] = abv[q] * out;
+            outp[q] = out;
+        }
+        if (!mbar_wait_bounded(&bar[1], 0)) {
+            if (threadIdx.x == 0) atomicOr(b.status, kStatusTmaTimeout);
+            mbar_wait_bounded(&bar[1], 0);
+            return;
+        }
+        float *gp = b.gpad + (long long)inst * g.fstride;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const float out = outp[q];
+            if (out == 0.0f) continue;
+            const int rr = rr0 + q * RS;
+            const int iz = row0 + rr;
+            const int j = jp + q * RS * g.pitch;
+            const float *sp1 = s_p1 + (rr + H) * kBoxX + sc;
+            float lx = fd_weight<H>(0) * sp1[0], lz = lx;
+#pragma unroll
+            for (int m = 1; m <= H; ++m) {
+                lx += fd_weight<H>(m) * (sp1[m] + sp1[-m]);
+                lz += fd_weight<H>(m) * (sp1[m * kBoxX] + sp1[-m * kBoxX]);
+            }
+            float d = 2.0f * vdv[q] * g.dt * (lx * rdx2 + lz * rdz2);
+            if (iz == g.s_iz && ix == g.s_ix0 + shot * g.ds) d += 2.0f * rik_prev * g.dt * vdv[q];
+            gp[j] += out * d;
+        }
+        return;
+    }
     float outv[R];
     int4 cpk[R];  // each row's cell facts, packed (cell_pack)
 #pragma unroll
