@@ -72,6 +72,19 @@ def fused_seconds(batches: list, cap_bytes: int, lib=None) -> float:
     return work + 2 * max(wave_steps, longest) * LAUNCH_OVERHEAD_S
 
 
+# A batch admitted beside running calls may be planned in the memory they
+# leave; it is held back instead when that plan would take more than this
+# factor of its time with the whole budget (tiny waves: every launch a
+# handful of solves), since waiting for the running calls frees the memory.
+SQUEEZE_LIMIT = 1.5
+
+
+def worth_starting(now_seconds: float, best_seconds: float, others_running: bool) -> bool:
+    """Start a batch planned in the memory free now (est. now_seconds), or
+    wait for running calls to free more (best_seconds with the whole budget)?"""
+    return not others_running or now_seconds <= SQUEEZE_LIMIT * best_seconds
+
+
 @dataclass
 class Plan:
     """How one batch runs: resident solves per wave, storage mode, bytes, cost."""
@@ -393,8 +406,10 @@ class FwiServer:
             if 0 < need <= cap:
                 batches = [(self._inv[name].params, n) for name, _, n in groups]
                 alone = [plan_batch(p, n, cap, self.lib) for p, n in batches]
-                if any(a is None for a in alone) or fused_seconds(batches, cap, self.lib) <= sum(
-                        a.est_seconds for a in alone):
+                t = fused_seconds(batches, cap, self.lib)
+                if self._running and not worth_starting(t, fused_seconds(batches, self.budget, self.lib), True):
+                    return None
+                if any(a is None for a in alone) or t <= sum(a.est_seconds for a in alone):
                     # room for every solve resident at once, capped by the arena
                     full = sum(_ws(self.lib, p.c(), n, 0, flags) for p, n in batches)
                     return groups, int(min(cap, full + (8 << 20)))
@@ -428,6 +443,10 @@ class FwiServer:
             name, group, n = groups[0]
             inv = self._inv[name]
             plan = plan_batch(inv.params, n, cap, self.lib)
+            if plan is not None and self._running:
+                best = plan_batch(inv.params, n, self.budget, self.lib)
+                if best is not None and not worth_starting(plan.est_seconds, best.est_seconds, True):
+                    break  # squeezed into tiny waves: wait for memory to free up
             if plan is None:
                 if not self._running:
                     for r in group:

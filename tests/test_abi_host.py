@@ -247,3 +247,19 @@ def test_fused_call_chosen_by_cost():
            (workloads.make_params(300, 600, 4500, 1e-3, 30, 8.0), 24)]
     alone = sum(plan_batch(p, n, cap // 2).est_seconds for p, n in big)
     assert fused_seconds(big, cap // 2) > alone
+
+
+def test_admission_waits_rather_than_squeezing():
+    """A batch planned in the little memory running calls leave (tiny waves)
+    waits for them; with nothing running, or with room, it starts."""
+    from geopvi_gb300 import workloads
+    from geopvi_gb300.scheduler import plan_batch, worth_starting
+    p = workloads.make_params(400, 800, 4363, 1e-3, 32, 8.0)
+    best = plan_batch(p, 8, 150 << 30)
+    squeezed = plan_batch(p, 8, 4 << 30)  # one resident solve, checkpointed
+    assert best is not None and squeezed is not None
+    assert squeezed.est_seconds > 3 * best.est_seconds
+    assert not worth_starting(squeezed.est_seconds, best.est_seconds, True)
+    assert worth_starting(squeezed.est_seconds, best.est_seconds, False)
+    roomy = plan_batch(p, 8, 120 << 30)
+    assert worth_starting(roomy.est_seconds, best.est_seconds, True)
