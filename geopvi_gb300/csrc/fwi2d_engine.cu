@@ -2038,6 +2038,11 @@ int gb_fwi2d_run_instances(const gb_fwi2d_instance *inst, int n, unsigned flags,
     if (st) return st;  // not reached: every instance was checked to fit alone
     cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
+    // A fused chunk copies its Ricker tables from pageable host memory, which
+    // a stream capture does not allow: refuse before anything is enqueued.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (!plan.chunks.empty() && (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone))
+        return GB_FWI2D_ENOTSUP;
     for (size_t c = 0; c < plan.chunks.size() && !st; ++c) {
         for (auto &f : plan.chunks[c]) {
             st = get_tables(f.d, f.tab);

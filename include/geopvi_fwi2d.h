@@ -155,7 +155,11 @@ size_t gb_fwi2d_instances_workspace_bytes(const gb_fwi2d_instance *inst, int n, 
  *
  * Every instance is checked before anything is enqueued: an invalid one
  * returns its status (GB_FWI2D_EINVAL; GB_FWI2D_ENOMEM when work_bytes is
- * below gb_fwi2d_instances_workspace_bytes) and nothing runs.  The
+ * below gb_fwi2d_instances_workspace_bytes) and nothing runs.  A fused call
+ * copies a small host table to the device, which stream capture does not
+ * allow: on a stream being captured it returns GB_FWI2D_ENOTSUP, again
+ * before anything is enqueued (GB_FWI2D_GRAPH runs the instances unfused,
+ * each captured and replayed as gb_fwi2d_batch does).  The
  * workspace's status word (gb_fwi2d_status) collects the flags of every
  * instance of the call.  Concurrency across streams and memory admission for
  * mixed workloads are geopvi_gb300/scheduler.py's. */
